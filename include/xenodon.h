@@ -1,0 +1,183 @@
+/*
+ * xenodon-gb300: C ABI of the GB300 volume ray-traversal library.
+ *
+ * Plain C types only: opaque handles, pointers and sizes.  Every function
+ * returns an int status (XN_OK = 0, negative = error); the message of the last
+ * error on the calling thread is available from xn_last_error().  No C++
+ * exception crosses this boundary.  Host buffers belong to the caller; device
+ * memory belongs to the library (a context and the volumes created from it),
+ * except for the xn_*_device entry points, which write into caller-owned
+ * device buffers on a caller-given CUDA stream.
+ *
+ * Each declaration names the reference interface it stands in for
+ * (paths relative to the reference project root).
+ */
+#ifndef XENODON_H
+#define XENODON_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#define XN_EXTERN extern "C"
+#else
+#define XN_EXTERN extern
+#endif
+#define XN_API XN_EXTERN __attribute__((visibility("default")))
+
+#define XN_ABI_VERSION 1
+
+/* ---- status codes ---- */
+enum {
+    XN_OK = 0,
+    XN_ERR_ARG = -1,       /* invalid argument */
+    XN_ERR_CUDA = -2,      /* a CUDA call failed */
+    XN_ERR_NOMEM = -3,     /* host or device allocation failed */
+    XN_ERR_FORMAT = -4,    /* malformed file or octree */
+    XN_ERR_BUDGET = -5,    /* the context's HBM budget does not admit the request */
+    XN_ERR_RAY_LIMIT = -6, /* a ray hit an iteration cap or a stack limit (output still written) */
+    XN_ERR_IO = -7,        /* file could not be opened, read or written */
+    XN_ERR_STATE = -8      /* call not valid in the current state */
+};
+
+/* Traversal algorithms, in the order of src/main_loop.cpp:37-43 (SHADER_OPTIONS). */
+typedef enum {
+    XN_DDA = 0,       /* resources/dda.comp */
+    XN_SVO_NAIVE = 1, /* resources/svo_naive.comp */
+    XN_ESVO = 2,      /* resources/esvo.comp */
+    XN_SVO_DF = 3,    /* resources/svo_df.comp */
+    XN_SVO_ROPE = 4   /* resources/svo_rope.comp */
+} xn_traversal;
+
+typedef enum { XN_VOLUME_GRID = 0, XN_VOLUME_SVO = 1 } xn_volume_kind;
+
+/* Octree types and split heuristics of `xenodon convert` (src/convert.cpp:24-37,
+ * src/model/Octree.h:16-20, src/model/OctreeConstruction.h:32-48). */
+typedef enum { XN_SVO_SPARSE = 0, XN_SVO_DAG = 1, XN_SVO_ROPE_TREE = 2 } xn_svo_type;
+typedef enum { XN_HEUR_CHANNEL_DIFF = 0, XN_HEUR_STD_DEV = 1 } xn_heuristic;
+
+typedef struct xn_ctx xn_ctx;
+typedef struct xn_volume xn_volume;
+
+/* src/camera/Camera.h:6-10; one line of a camera script (ScriptCameraController.cpp:17-40). */
+typedef struct {
+    float forward[3];
+    float up[3];
+    float translation[3]; /* raw: the library divides by voxel_ratio (src/render/Renderer.cpp:62) */
+} xn_camera;
+
+/* vk::Rect2D as used by the UBO of resources/common.glsl:12-15,29-33. */
+typedef struct {
+    int32_t x, y;
+    uint32_t width, height;
+} xn_rect;
+
+/* UBO contents (resources/common.glsl:17-21,29-33; src/render/RenderContext.h:16-20).
+ * model_dim is taken from the volume. */
+typedef struct {
+    xn_rect output_region;  /* the pixels this call renders */
+    xn_rect display_region; /* the union rectangle uv is computed against */
+    float voxel_ratio[3];   /* --voxel-ratio, default 1:1:1 */
+    float emission_coeff;   /* -e, default 1 */
+} xn_params;
+
+typedef struct {
+    int kind;              /* xn_volume_kind */
+    uint32_t dim[3];       /* grid dimensions, or side^3 for an octree */
+    uint64_t side;         /* octree side (power of two), 0 for grids */
+    uint64_t n_nodes;      /* octree nodes in the reference layout, 0 for grids */
+    uint64_t device_bytes; /* HBM held by this volume */
+    int has_ropes;         /* octree leaves carry rope links (svo-rope is valid) */
+} xn_volume_info;
+
+/* ConstructionStats (src/model/OctreeConstruction.h:50-62) plus the result size. */
+typedef struct {
+    uint64_t total_leaves;
+    uint64_t unique_leaves;
+    uint64_t total_nodes;
+    uint64_t depth;
+    uint64_t side;
+    uint64_t n_nodes;
+} xn_build_stats;
+
+/* ------------------------------------------------------------- context --- */
+
+/* Replaces the per-device Vulkan setup of src/backend/headless/HeadlessOutput.cpp:38-63
+ * and src/render/Renderer.cpp:17-30: one CUDA device context.  hbm_budget_bytes
+ * caps what volumes and render targets of this context may hold (0 = no cap). */
+XN_API int xn_create(int device, uint64_t hbm_budget_bytes, xn_ctx** out);
+XN_API int xn_destroy(xn_ctx* ctx);
+/* Message of the last failed call on this thread ("" if none). */
+XN_API const char* xn_last_error(void);
+XN_API int xn_abi_version(void);
+/* Device memory currently held by the context's volumes and buffers. */
+XN_API int xn_ctx_memory(const xn_ctx* ctx, uint64_t* used_bytes, uint64_t* budget_bytes);
+
+/* -------------------------------------------------------------- volumes --- */
+
+/* Replaces DdaRaytraceAlgorithm::upload_resources / DdaRaytraceResources
+ * (src/render/DdaRaytraceAlgorithm.cpp:15-97): uploads an RGBA8 grid, x fastest
+ * (src/model/Grid.h:50-52), dx*dy*dz*4 bytes from host memory. */
+XN_API int xn_volume_upload_grid(xn_ctx* ctx, const uint8_t* rgba, uint32_t dx, uint32_t dy,
+                                 uint32_t dz, xn_volume** out);
+
+/* Replaces SvoRaytraceAlgorithm::upload_resources / SvoRaytraceResources
+ * (src/render/SvoRaytraceAlgorithm.cpp:12-48): uploads n_nodes nodes of 10
+ * little-endian u32 words (resources/octree.glsl:6-10, src/model/Octree.h:35-45).
+ * The octree is validated (every child index < n_nodes) and re-laid out on the
+ * device for traversal. */
+XN_API int xn_volume_upload_svo(xn_ctx* ctx, const uint32_t* nodes, uint64_t n_nodes, uint64_t side,
+                                xn_volume** out);
+XN_API int xn_volume_release(xn_volume* vol);
+XN_API int xn_volume_info_get(const xn_volume* vol, xn_volume_info* info);
+
+/* -------------------------------------------------------------- render --- */
+
+/* Replaces Renderer::render + HeadlessOutput::synchronize/download
+ * (src/render/Renderer.cpp:55-103, src/backend/headless/HeadlessOutput.cpp:90-136):
+ * renders params->output_region with the given traversal and copies the result
+ * to host memory.
+ *   out_rgba      width*height*4 bytes (row pitch width*4), or NULL
+ *   out_emission  width*height*3 floats: colour after the emission coefficient,
+ *                 before the UNORM clamp, or NULL
+ *   kernel_ms     device time of the traversal kernel (the quantity of
+ *                 src/render/RenderStats.cpp:59-83), or NULL
+ * Returns XN_ERR_RAY_LIMIT, with the outputs written, when a ray hit an
+ * iteration cap (where the reference shader would not terminate). */
+XN_API int xn_render(xn_ctx* ctx, const xn_volume* vol, int traversal, const xn_camera* cam,
+                     const xn_params* params, uint8_t* out_rgba, float* out_emission,
+                     float* kernel_ms);
+
+/* Device-side form of xn_render: writes into caller-owned device buffers on
+ * `stream` (a cudaStream_t, NULL = the legacy default stream) and returns
+ * without synchronising.  d_loads, when not NULL, receives per ray the number
+ * of 32-bit words the reference shader reads (texels for DDA, node words for
+ * the octree traversals). */
+XN_API int xn_render_device(xn_ctx* ctx, const xn_volume* vol, int traversal, const xn_camera* cam,
+                            const xn_params* params, void* d_rgba, float* d_emission,
+                            uint32_t* d_loads, void* stream);
+
+/* Error bits raised by rays since the last call (1 = iteration cap, 2 = stack
+ * limit); reset clears them.  Synchronises the context's device. */
+XN_API int xn_ray_errors(xn_ctx* ctx, uint32_t* bits, int reset);
+
+/* ------------------------------------------------------------ SVO build --- */
+
+/* Replaces build_octree + Octree::generate_ropes as driven by `xenodon convert`
+ * (src/model/OctreeConstruction.h:197-237, src/model/Octree.cpp:181-201,
+ * src/convert.cpp:76-85): builds the octree of an RGBA8 grid on the GPU, bit
+ * for bit the reference's node array.  *nodes_out is malloc'd host memory
+ * (n_nodes*10 u32) that the caller frees with xn_free. */
+XN_API int xn_build_svo(xn_ctx* ctx, const uint8_t* rgba, uint32_t dx, uint32_t dy, uint32_t dz,
+                        int type, int heuristic, double threshold, uint32_t** nodes_out,
+                        xn_build_stats* stats);
+XN_API void xn_free(void* p);
+
+/* --------------------------------------------------------- file formats --- */
+
+/* Octree::load_svo / save_svo (src/model/Octree.cpp:50-114): "XNDN-SVO", u64
+ * side, u64 node count, nodes of 10 LE u32.  load returns malloc'd nodes. */
+XN_API int xn_svo_load(const char* path, uint32_t** nodes_out, uint64_t* n_nodes, uint64_t* side);
+XN_API int xn_svo_save(const char* path, const uint32_t* nodes, uint64_t n_nodes, uint64_t side);
+
+#endif

@@ -1,0 +1,190 @@
+"""Parity of the CUDA traversal kernels with the oracle, through the C ABI.
+
+Tolerances (written here, checked per traversal):
+  * RGBA8 image vs the FP32 oracle: identical on >= 99.99% of pixels and
+    within 1 LSB per channel on all of them;
+  * per-ray emission vs the FP32 oracle: >= 99.9% of rays bit-identical and
+    every ray within 1e-5 relative (+1e-7 absolute);
+  * per-ray emission vs the FP64 re-trace: 1e-5 relative is met by at least as
+    many rays as the reference algorithm in FP32 (the FP32 oracle) meets it,
+    less 0.1%; the shaders' own FP32 stepping error keeps a few per cent of
+    rays above 1e-5, so 1e-5 cannot be required of every ray;
+  * words read per ray (the roofline's algorithmic bytes): equal to the
+    oracle's count on every ray.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+TRAV = ("dda", "svo-naive", "esvo", "svo-df", "svo-rope")
+
+
+def _params_pair(xg, w, h, e=10.0, ratio=(1.0, 1.0, 1.0), out_off=(0, 0), out_ext=None, disp_off=(0, 0),
+                 disp_ext=None):
+    p = xg.make_params(w, h, e, ratio, out_off, out_ext, disp_off, disp_ext)
+    v = oracle.make_view(w, h, e, ratio, out_off, out_ext, disp_off, disp_ext)
+    return p, v
+
+
+def _gpu_counts(ctx, vol, trav, cam, params):
+    import torch
+    w, h = params.output_region.width, params.output_region.height
+    rgba = torch.empty((h, w), dtype=torch.int32, device="cuda")
+    loads = torch.empty((h, w), dtype=torch.int32, device="cuda")
+    em = torch.empty((h, w, 3), dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream()
+    ctx.render_device(vol, trav, cam, params, rgba.data_ptr(), em.data_ptr(), loads.data_ptr(), s.cuda_stream)
+    torch.cuda.synchronize()
+    return rgba, em.cpu().numpy(), loads.cpu().numpy().view(np.uint32)
+
+
+def check_parity(ctx, trav, cam_tuple, params, view, grid=None, nodes=None, side=None, vol=None, label=""):
+    import xenodon_gb300 as xg
+    if vol is None:
+        vol = ctx.upload_grid(grid) if trav == "dda" else ctx.upload_svo(nodes, side)
+    cam = xg.make_camera(*cam_tuple)
+    ocam = oracle.make_camera(*cam_tuple)
+    rgba, em, ms = ctx.render(vol, trav, cam, params, emission=True)
+    ref = oracle.render(trav, grid=grid, nodes=nodes, camera=ocam, view=view)
+    ref64 = oracle.render(trav, grid=grid, nodes=nodes, camera=ocam, view=view, f64=True, want_loads=False)
+    assert ref["errors"] == 0, label
+    d = np.abs(rgba.astype(np.int32) - ref["rgba"].astype(np.int32))
+    assert d.max() <= 1, f"{label} {trav}: RGBA off by {d.max()}"
+    same_px = np.all(d == 0, axis=2).mean()
+    assert same_px >= 0.9999, f"{label} {trav}: only {same_px:.6f} of pixels identical"
+    e32 = ref["emission"]
+    exact = (em == e32).all(axis=2).mean()
+    assert exact >= 0.999, f"{label} {trav}: only {exact:.5f} of rays bit-identical"
+    assert np.all(np.abs(em - e32) <= 1e-5 * np.abs(e32) + 1e-7), f"{label} {trav}: emission beyond 1e-5"
+    e64 = ref64["emission"]
+    sig = np.abs(e64) > 1e-3 * max(1e-30, np.abs(e64).max())
+    if sig.any():
+        rel_gpu = (np.abs(em.astype(np.float64) - e64) / np.abs(e64).clip(1e-30))[sig]
+        rel_ref = (np.abs(e32.astype(np.float64) - e64) / np.abs(e64).clip(1e-30))[sig]
+        assert (rel_gpu <= 1e-5).mean() >= (rel_ref <= 1e-5).mean() - 1e-3, f"{label} {trav}: worse than FP32 reference"
+    _, em2, loads = _gpu_counts(ctx, vol, trav, cam, params)
+    assert np.array_equal(loads, ref["loads"]), f"{label} {trav}: load counts differ"
+    assert np.array_equal(em2, em), f"{label} {trav}: counting variant changed the result"
+    return rgba, ms
+
+
+@pytest.fixture(scope="module")
+def blob_volumes():
+    from xenodon_gb300 import volumes
+    g = volumes.blobs(64, seed=0)
+    nodes, st = oracle.build_svo(g, "rope")
+    return g, nodes, st["side"]
+
+
+CAMS = {
+    "front": ((0, 0, -0.8660254), (0, 1, 0), (0.5, 0.5, 2.5)),
+    "oblique": ((0.35, -0.2, -0.91), (0.0, 0.976, -0.215), (0.2, 0.8, 2.0)),
+    "inside": ((0.6, 0.3, 0.74), (-0.2, 0.95, 0.0), (0.45, 0.55, 0.5)),
+    "grazing": ((1.0, 0.0, 0.0), (0, 1, 0), (-1.0, 0.5, 0.5)),
+}
+
+
+@pytest.mark.parametrize("cam", list(CAMS))
+@pytest.mark.parametrize("trav", TRAV)
+def test_parity_blobs(ctx, blob_volumes, trav, cam):
+    import xenodon_gb300 as xg
+    g, nodes, side = blob_volumes
+    p, v = _params_pair(xg, 96, 64)
+    check_parity(ctx, trav, CAMS[cam], p, v, grid=g, nodes=nodes, side=side, label=f"blobs/{cam}")
+
+
+@pytest.mark.parametrize("trav", TRAV)
+def test_parity_ct_shell_non_cubic(ctx, trav):
+    import xenodon_gb300 as xg
+    from xenodon_gb300 import volumes
+    g = volumes.ct_shell(64, 45, 64, seed=1, device="cpu")
+    nodes, st = oracle.build_svo(g, "rope")
+    cam = ((0.3, -0.1, 0.95), (0, 1, 0.1), (0.3, 0.45, -1.2))
+    p, v = _params_pair(xg, 80, 60, e=10.0)
+    check_parity(ctx, trav, cam, p, v, grid=g, nodes=nodes, side=st["side"], label="ct")
+
+
+@pytest.mark.parametrize("trav", ("svo-naive", "esvo", "svo-df"))
+def test_parity_dag_tree(ctx, trav):
+    # DAG trees share subtrees; naive / df / esvo traverse them unchanged
+    import xenodon_gb300 as xg
+    from xenodon_gb300 import volumes
+    g = volumes.random_grid(32, 32, 32, seed=9, density=0.4, levels=3)
+    nodes, st = oracle.build_svo(g, "dag")
+    p, v = _params_pair(xg, 64, 64, e=5.0)
+    check_parity(ctx, trav, CAMS["oblique"], p, v, nodes=nodes, side=st["side"], label="dag")
+
+
+@pytest.mark.parametrize("trav", TRAV)
+def test_parity_subregion_and_voxel_ratio(ctx, blob_volumes, trav):
+    # an output region inside a larger display region (one device block of a
+    # multi-device headless.conf) with an anisotropic --voxel-ratio
+    import xenodon_gb300 as xg
+    g, nodes, side = blob_volumes
+    p, v = _params_pair(xg, 0, 0, e=7.0, ratio=(1.0, 1.5, 0.75), out_off=(40, 16), out_ext=(50, 37),
+                        disp_off=(0, 0), disp_ext=(128, 72))
+    check_parity(ctx, trav, CAMS["front"], p, v, grid=g, nodes=nodes, side=side, label="subregion")
+
+
+@pytest.mark.parametrize("trav", ("svo-naive", "esvo", "svo-df", "svo-rope"))
+def test_parity_leaf_root_and_depth_one(ctx, trav):
+    import xenodon_gb300 as xg
+    g = np.zeros((2, 2, 2, 4), np.uint8)
+    g[..., 3] = 255
+    g[0, 1, 1, :3] = (250, 10, 10)
+    for grid in (np.full((4, 4, 4, 4), 77, np.uint8), g):
+        nodes, st = oracle.build_svo(grid, "rope")
+        p, v = _params_pair(xg, 32, 32, e=3.0)
+        check_parity(ctx, trav, CAMS["oblique"], p, v, nodes=nodes, side=st["side"], label="tiny")
+
+
+def test_svo_rope_on_a_tree_without_ropes_matches_reference(ctx, blob_volumes):
+    # without ropes every leaf's neighbour word is 0 (the root): the reference
+    # shader stops after the first leaf, and so do we
+    import xenodon_gb300 as xg
+    g, _, _ = blob_volumes
+    nodes, st = oracle.build_svo(g, "sparse")
+    p, v = _params_pair(xg, 48, 48)
+    check_parity(ctx, "svo-rope", CAMS["front"], p, v, nodes=nodes, side=st["side"], label="no-ropes")
+
+
+def test_volume_kind_mismatch_is_rejected(ctx, blob_volumes):
+    import xenodon_gb300 as xg
+    g, nodes, side = blob_volumes
+    vg = ctx.upload_grid(g)
+    vs = ctx.upload_svo(nodes, side)
+    cam = xg.make_camera(*CAMS["front"])
+    p = xg.make_params(8, 8)
+    for vol, trav in ((vg, "esvo"), (vs, "dda")):
+        with pytest.raises(xg.XenodonError) as e:
+            ctx.render(vol, trav, cam, p)
+        assert e.value.code == xg.XN_ERR_ARG
+    assert vs.info()["has_ropes"] and vs.info()["n_nodes"] == nodes.shape[0]
+
+
+def test_malformed_octree_upload_is_rejected(ctx, blob_volumes):
+    import xenodon_gb300 as xg
+    _, nodes, side = blob_volumes
+    bad = nodes.copy()
+    bad[3, 2] = nodes.shape[0]  # child index out of range
+    with pytest.raises(xg.XenodonError) as e:
+        ctx.upload_svo(bad, side)
+    assert e.value.code == xg.XN_ERR_FORMAT
+
+
+def test_hbm_budget_refuses_uploads(built_library, blob_volumes):
+    import torch
+    import xenodon_gb300 as xg
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    g, _, _ = blob_volumes
+    with xg.Context(0, hbm_budget=g.nbytes // 2) as c:
+        with pytest.raises(xg.XenodonError) as e:
+            c.upload_grid(g)
+        assert e.value.code == xg.XN_ERR_BUDGET
+        assert c.memory()[0] < g.nbytes // 2

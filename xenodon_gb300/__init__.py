@@ -1,0 +1,272 @@
+"""xenodon_gb300: GB300-native volume ray traversal (Xenodon's hot path).
+
+Thin ctypes bindings over the C ABI in include/xenodon.h, implemented by
+``xenodon_gb300/lib/libxenodon.so`` (CUDA kernels for sm_103a + host code).
+There is no CPU fallback: if the library is missing, importing the bindings
+raises.  Build it with ``python -m xenodon_gb300.build``.
+
+Traversal names follow ``xenodon render -s`` (src/main_loop.cpp:37-43).
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libxenodon.so"
+CLI_PATH = PKG / "bin" / "xenodon"
+
+TRAVERSALS = {"dda": 0, "svo-naive": 1, "esvo": 2, "svo-df": 3, "svo-rope": 4}
+SVO_TRAVERSALS = ("svo-naive", "esvo", "svo-df", "svo-rope")
+SVO_TYPES = {"sparse": 0, "dag": 1, "rope": 2}
+HEURISTICS = {"chan-diff": 0, "std-dev": 1}
+
+XN_OK = 0
+XN_ERR_ARG, XN_ERR_CUDA, XN_ERR_NOMEM, XN_ERR_FORMAT = -1, -2, -3, -4
+XN_ERR_BUDGET, XN_ERR_RAY_LIMIT, XN_ERR_IO, XN_ERR_STATE = -5, -6, -7, -8
+
+# Every symbol include/xenodon.h declares.
+EXPORTS = (
+    "xn_create", "xn_destroy", "xn_last_error", "xn_abi_version", "xn_ctx_memory",
+    "xn_volume_upload_grid", "xn_volume_upload_svo", "xn_volume_release", "xn_volume_info_get",
+    "xn_render", "xn_render_device", "xn_ray_errors", "xn_build_svo", "xn_free",
+    "xn_svo_load", "xn_svo_save",
+)
+
+
+class XenodonError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{message} (status {code})")
+        self.code = code
+
+
+class Camera(ctypes.Structure):
+    _fields_ = [("forward", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
+                ("translation", ctypes.c_float * 3)]
+
+
+class Rect(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_int32), ("y", ctypes.c_int32),
+                ("width", ctypes.c_uint32), ("height", ctypes.c_uint32)]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("output_region", Rect), ("display_region", Rect),
+                ("voxel_ratio", ctypes.c_float * 3), ("emission_coeff", ctypes.c_float)]
+
+
+class VolumeInfo(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("dim", ctypes.c_uint32 * 3), ("side", ctypes.c_uint64),
+                ("n_nodes", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64), ("has_ropes", ctypes.c_int)]
+
+
+class BuildStats(ctypes.Structure):
+    _fields_ = [("total_leaves", ctypes.c_uint64), ("unique_leaves", ctypes.c_uint64),
+                ("total_nodes", ctypes.c_uint64), ("depth", ctypes.c_uint64),
+                ("side", ctypes.c_uint64), ("n_nodes", ctypes.c_uint64)]
+
+
+_lib = None
+
+
+def load_library(path: Path | str | None = None) -> ctypes.CDLL:
+    """Load libxenodon.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(f"{p} is missing: build it with `python -m xenodon_gb300.build`")
+    l = ctypes.CDLL(str(p))
+    P = ctypes.POINTER
+    vp, u32, u64, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+    sig = {
+        "xn_create": (i32, [i32, u64, P(vp)]),
+        "xn_destroy": (i32, [vp]),
+        "xn_last_error": (ctypes.c_char_p, []),
+        "xn_abi_version": (i32, []),
+        "xn_ctx_memory": (i32, [vp, P(u64), P(u64)]),
+        "xn_volume_upload_grid": (i32, [vp, vp, u32, u32, u32, P(vp)]),
+        "xn_volume_upload_svo": (i32, [vp, vp, u64, u64, P(vp)]),
+        "xn_volume_release": (i32, [vp]),
+        "xn_volume_info_get": (i32, [vp, P(VolumeInfo)]),
+        "xn_render": (i32, [vp, vp, i32, P(Camera), P(Params), vp, vp, P(ctypes.c_float)]),
+        "xn_render_device": (i32, [vp, vp, i32, P(Camera), P(Params), vp, vp, vp, vp]),
+        "xn_ray_errors": (i32, [vp, P(u32), i32]),
+        "xn_build_svo": (i32, [vp, vp, u32, u32, u32, i32, i32, ctypes.c_double, P(P(u32)), P(BuildStats)]),
+        "xn_free": (None, [vp]),
+        "xn_svo_load": (i32, [ctypes.c_char_p, P(P(u32)), P(u64), P(u64)]),
+        "xn_svo_save": (i32, [ctypes.c_char_p, vp, u64, u64]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(l, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = l
+    return l
+
+
+def _check(code: int) -> int:
+    if code != XN_OK:
+        raise XenodonError(code, load_library().xn_last_error().decode(errors="replace"))
+    return code
+
+
+def make_camera(forward, up, translation) -> Camera:
+    c = Camera()
+    c.forward[:] = [float(v) for v in forward]
+    c.up[:] = [float(v) for v in up]
+    c.translation[:] = [float(v) for v in translation]
+    return c
+
+
+def make_params(width, height, emission_coeff=1.0, voxel_ratio=(1.0, 1.0, 1.0), output_offset=(0, 0),
+                output_extent=None, display_offset=(0, 0), display_extent=None) -> Params:
+    p = Params()
+    ow, oh = output_extent or (width, height)
+    dw, dh = display_extent or (width, height)
+    p.output_region = Rect(int(output_offset[0]), int(output_offset[1]), int(ow), int(oh))
+    p.display_region = Rect(int(display_offset[0]), int(display_offset[1]), int(dw), int(dh))
+    p.voxel_ratio[:] = [float(v) for v in voxel_ratio]
+    p.emission_coeff = float(emission_coeff)
+    return p
+
+
+def _traversal(t) -> int:
+    return TRAVERSALS[t] if isinstance(t, str) else int(t)
+
+
+class Volume:
+    """A volume resident in HBM (grid or octree)."""
+
+    def __init__(self, ctx: "Context", handle: ctypes.c_void_p):
+        self.ctx = ctx
+        self.handle = handle
+
+    def info(self) -> dict:
+        vi = VolumeInfo()
+        _check(load_library().xn_volume_info_get(self.handle, ctypes.byref(vi)))
+        return {"kind": "grid" if vi.kind == 0 else "svo", "dim": tuple(vi.dim), "side": vi.side,
+                "n_nodes": vi.n_nodes, "device_bytes": vi.device_bytes, "has_ropes": bool(vi.has_ropes)}
+
+    def release(self) -> None:
+        if self.handle:
+            load_library().xn_volume_release(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            if self.handle and self.ctx.handle:
+                self.release()
+        except Exception:
+            pass
+
+
+class Context:
+    """One CUDA device context (xn_create)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        _check(self.lib.xn_create(device, hbm_budget, ctypes.byref(h)))
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.xn_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def memory(self) -> tuple[int, int]:
+        used, budget = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(self.lib.xn_ctx_memory(self.handle, ctypes.byref(used), ctypes.byref(budget)))
+        return used.value, budget.value
+
+    def upload_grid(self, grid: np.ndarray) -> Volume:
+        """grid: uint8 (dz, dy, dx, 4), x fastest."""
+        g = np.ascontiguousarray(grid, dtype=np.uint8)
+        if g.ndim != 4 or g.shape[3] != 4:
+            raise ValueError("grid must have shape (dz, dy, dx, 4)")
+        h = ctypes.c_void_p()
+        _check(self.lib.xn_volume_upload_grid(self.handle, g.ctypes.data, g.shape[2], g.shape[1], g.shape[0],
+                                              ctypes.byref(h)))
+        return Volume(self, h)
+
+    def upload_svo(self, nodes: np.ndarray, side: int) -> Volume:
+        """nodes: uint32 (n, 10) in the reference layout."""
+        n = np.ascontiguousarray(nodes, dtype=np.uint32).reshape(-1, 10)
+        h = ctypes.c_void_p()
+        _check(self.lib.xn_volume_upload_svo(self.handle, n.ctypes.data, n.shape[0], int(side), ctypes.byref(h)))
+        return Volume(self, h)
+
+    def render(self, vol: Volume, traversal, camera: Camera, params: Params, emission: bool = False,
+               allow_ray_limit: bool = False):
+        """Render to host memory.  Returns (rgba (h, w, 4) u8, emission (h, w, 3) f32 or None, kernel_ms)."""
+        w, h = params.output_region.width, params.output_region.height
+        rgba = np.empty((h, w, 4), np.uint8)
+        em = np.empty((h, w, 3), np.float32) if emission else None
+        ms = ctypes.c_float()
+        r = self.lib.xn_render(self.handle, vol.handle, _traversal(traversal), ctypes.byref(camera),
+                               ctypes.byref(params), rgba.ctypes.data, em.ctypes.data if em is not None else None,
+                               ctypes.byref(ms))
+        if not (allow_ray_limit and r == XN_ERR_RAY_LIMIT):
+            _check(r)
+        return rgba, em, ms.value
+
+    def render_device(self, vol: Volume, traversal, camera: Camera, params: Params, d_rgba: int,
+                      d_emission: int | None = None, d_loads: int | None = None, stream: int | None = None) -> None:
+        """Launch into caller-owned device buffers (raw device pointers) on `stream`."""
+        _check(self.lib.xn_render_device(self.handle, vol.handle, _traversal(traversal), ctypes.byref(camera),
+                                         ctypes.byref(params), d_rgba, d_emission, d_loads, stream))
+
+    def ray_errors(self, reset: bool = True) -> int:
+        bits = ctypes.c_uint32()
+        _check(self.lib.xn_ray_errors(self.handle, ctypes.byref(bits), int(reset)))
+        return bits.value
+
+    def build_svo(self, grid: np.ndarray, svo_type="sparse", heuristic="chan-diff", threshold=0.0):
+        """Build the reference octree of an RGBA8 grid on the GPU.  Returns (nodes (n, 10) u32, stats)."""
+        g = np.ascontiguousarray(grid, dtype=np.uint8)
+        out = ctypes.POINTER(ctypes.c_uint32)()
+        st = BuildStats()
+        _check(self.lib.xn_build_svo(self.handle, g.ctypes.data, g.shape[2], g.shape[1], g.shape[0],
+                                     SVO_TYPES[svo_type], HEURISTICS[heuristic], float(threshold),
+                                     ctypes.byref(out), ctypes.byref(st)))
+        n = st.n_nodes
+        try:
+            arr = np.ctypeslib.as_array(out, shape=(n * 10,)).copy().reshape(n, 10) if n else np.zeros((0, 10), np.uint32)
+        finally:
+            self.lib.xn_free(out)
+        return arr, {f: int(getattr(st, f)) for f, _ in BuildStats._fields_}
+
+
+def svo_load(path) -> tuple[np.ndarray, int]:
+    lib = load_library()
+    out = ctypes.POINTER(ctypes.c_uint32)()
+    n, side = ctypes.c_uint64(), ctypes.c_uint64()
+    _check(lib.xn_svo_load(str(path).encode(), ctypes.byref(out), ctypes.byref(n), ctypes.byref(side)))
+    try:
+        arr = np.ctypeslib.as_array(out, shape=(n.value * 10,)).copy().reshape(-1, 10) if n.value else \
+            np.zeros((0, 10), np.uint32)
+    finally:
+        lib.xn_free(out)
+    return arr, side.value
+
+
+def svo_save(path, nodes: np.ndarray, side: int) -> None:
+    n = np.ascontiguousarray(nodes, dtype=np.uint32).reshape(-1, 10)
+    _check(load_library().xn_svo_save(str(path).encode(), n.ctypes.data, n.shape[0], int(side)))

@@ -1,0 +1,390 @@
+// C-ABI layer (include/xenodon.h): contexts, volumes, render entry points.
+//
+// Replaces the reference's per-device Vulkan plumbing
+// (src/render/Renderer.cpp, src/render/DdaRaytraceAlgorithm.cpp,
+// src/render/SvoRaytraceAlgorithm.cpp, src/backend/headless/HeadlessOutput.cpp)
+// with one CUDA device context per xn_ctx.  No C++ exception crosses the ABI:
+// every entry point catches, records a message for xn_last_error() and
+// returns a status.
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "../../include/xenodon.h"
+#include "xn_internal.h"
+#include "xn_ctx.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+}  // namespace
+
+namespace xn {
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(e == cudaErrorMemoryAllocation ? XN_ERR_NOMEM : XN_ERR_CUDA, "%s: %s", what,
+                cudaGetErrorString(e));
+}
+
+int Ctx::device_alloc(void** p, uint64_t bytes, const char* what) {
+    *p = nullptr;
+    if (bytes == 0) return XN_OK;
+    uint64_t cur = used.load();
+    if (budget && cur + bytes > budget)
+        return fail(XN_ERR_BUDGET, "%s: %llu bytes exceed the HBM budget (%llu of %llu bytes in use)", what,
+                    (unsigned long long)bytes, (unsigned long long)cur, (unsigned long long)budget);
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_fail(e, what);
+    }
+    used += bytes;
+    return XN_OK;
+}
+
+void Ctx::device_free(void* p, uint64_t bytes) {
+    if (!p) return;
+    cudaFree(p);
+    used -= bytes;
+}
+
+int Ctx::ensure_buffer(DeviceBuffer& b, uint64_t bytes, const char* what) {
+    if (b.bytes >= bytes) return XN_OK;
+    device_free(b.ptr, b.bytes);
+    b.ptr = nullptr;
+    b.bytes = 0;
+    int r = device_alloc(&b.ptr, bytes, what);
+    if (r == XN_OK) b.bytes = bytes;
+    return r;
+}
+
+void Ctx::release_extra() {}
+
+int Ctx::activate() {
+    cudaError_t e = cudaSetDevice(device);
+    return e == cudaSuccess ? XN_OK : cuda_fail(e, "cudaSetDevice");
+}
+
+}  // namespace xn
+
+using namespace xn;
+
+// ---------------------------------------------------------------- context ---
+
+XN_API const char* xn_last_error(void) { return g_last_error.c_str(); }
+
+XN_API int xn_abi_version(void) { return XN_ABI_VERSION; }
+
+XN_API int xn_create(int device, uint64_t hbm_budget_bytes, xn_ctx** out) {
+    if (!out) return fail(XN_ERR_ARG, "xn_create: out is NULL");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) return cuda_fail(e, "xn_create: cudaGetDeviceCount");
+    if (device < 0 || device >= count) return fail(XN_ERR_ARG, "xn_create: no CUDA device %d (%d present)", device, count);
+    Ctx* c = new (std::nothrow) Ctx();
+    if (!c) return fail(XN_ERR_NOMEM, "xn_create: out of host memory");
+    c->device = device;
+    c->budget = hbm_budget_bytes;
+    int r = c->activate();
+    if (r) { delete c; return r; }
+    if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess) {
+        r = cuda_fail(e, "xn_create");
+        xn_destroy(reinterpret_cast<xn_ctx*>(c));
+        return r;
+    }
+    r = c->device_alloc(reinterpret_cast<void**>(&c->d_err), sizeof(uint32_t), "xn_create: error word");
+    if (r) { xn_destroy(reinterpret_cast<xn_ctx*>(c)); return r; }
+    cudaMemsetAsync(c->d_err, 0, sizeof(uint32_t), c->stream);
+    cudaStreamSynchronize(c->stream);
+    *out = reinterpret_cast<xn_ctx*>(c);
+    return XN_OK;
+}
+
+XN_API int xn_destroy(xn_ctx* h) {
+    if (!h) return XN_OK;
+    Ctx* c = reinterpret_cast<Ctx*>(h);
+    c->activate();
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->device_free(c->out_rgba.ptr, c->out_rgba.bytes);
+    c->device_free(c->out_emission.ptr, c->out_emission.bytes);
+    c->device_free(c->d_err, sizeof(uint32_t));
+    c->release_extra();
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return XN_OK;
+}
+
+XN_API int xn_ctx_memory(const xn_ctx* h, uint64_t* used_bytes, uint64_t* budget_bytes) {
+    if (!h) return fail(XN_ERR_ARG, "xn_ctx_memory: ctx is NULL");
+    const Ctx* c = reinterpret_cast<const Ctx*>(h);
+    if (used_bytes) *used_bytes = c->used.load();
+    if (budget_bytes) *budget_bytes = c->budget;
+    return XN_OK;
+}
+
+// ---------------------------------------------------------------- volumes ---
+
+namespace {
+
+__global__ void validate_nodes_kernel(const uint32_t* w, uint64_t n, uint32_t* bad) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    uint32_t local = 0;
+    for (; i < n * 8; i += stride) {
+        uint64_t node = i >> 3, k = i & 7;
+        if (w[node * 10 + k] >= n) local = 1;
+    }
+    if (local) atomicOr(bad, 1u);
+}
+
+__global__ void detect_ropes_kernel(const uint32_t* w, uint64_t n, uint32_t* any) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    uint32_t local = 0;
+    for (; i < n; i += stride) {
+        const uint32_t* p = w + i * 10;
+        if (p[9] >= 0x80000000u && (p[0] | p[1] | p[2] | p[3] | p[4] | p[5])) local = 1;
+    }
+    if (local) atomicOr(any, 1u);
+}
+
+}  // namespace
+
+XN_API int xn_volume_upload_grid(xn_ctx* h, const uint8_t* rgba, uint32_t dx, uint32_t dy, uint32_t dz,
+                                 xn_volume** out) {
+    if (!h || !rgba || !out) return fail(XN_ERR_ARG, "xn_volume_upload_grid: NULL argument");
+    *out = nullptr;
+    if (!dx || !dy || !dz) return fail(XN_ERR_ARG, "xn_volume_upload_grid: empty grid %ux%ux%u", dx, dy, dz);
+    if ((uint64_t)dx + dy + dz > (1ull << 30)) return fail(XN_ERR_ARG, "xn_volume_upload_grid: grid too large");
+    Ctx* c = reinterpret_cast<Ctx*>(h);
+    std::lock_guard<std::mutex> lk(c->mu);
+    int r = c->activate();
+    if (r) return r;
+    Volume* v = new (std::nothrow) Volume();
+    if (!v) return fail(XN_ERR_NOMEM, "xn_volume_upload_grid: out of host memory");
+    v->ctx = c;
+    v->kind = XN_VOLUME_GRID;
+    v->dim[0] = dx;
+    v->dim[1] = dy;
+    v->dim[2] = dz;
+    v->bytes = (uint64_t)dx * dy * dz * 4;
+    r = c->device_alloc(&v->data, v->bytes, "xn_volume_upload_grid");
+    if (r) { delete v; return r; }
+    cudaError_t e = cudaMemcpyAsync(v->data, rgba, v->bytes, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        c->device_free(v->data, v->bytes);
+        delete v;
+        return cuda_fail(e, "xn_volume_upload_grid: copy");
+    }
+    *out = reinterpret_cast<xn_volume*>(v);
+    return XN_OK;
+}
+
+XN_API int xn_volume_upload_svo(xn_ctx* h, const uint32_t* nodes, uint64_t n_nodes, uint64_t side, xn_volume** out) {
+    if (!h || !nodes || !out) return fail(XN_ERR_ARG, "xn_volume_upload_svo: NULL argument");
+    *out = nullptr;
+    if (n_nodes == 0) return fail(XN_ERR_FORMAT, "xn_volume_upload_svo: octree has no nodes");
+    if (n_nodes > 0xFFFFFFFFull) return fail(XN_ERR_FORMAT, "xn_volume_upload_svo: more than 2^32 nodes need the 64-bit format");
+    Ctx* c = reinterpret_cast<Ctx*>(h);
+    std::lock_guard<std::mutex> lk(c->mu);
+    int r = c->activate();
+    if (r) return r;
+    Volume* v = new (std::nothrow) Volume();
+    if (!v) return fail(XN_ERR_NOMEM, "xn_volume_upload_svo: out of host memory");
+    v->ctx = c;
+    v->kind = XN_VOLUME_SVO;
+    v->side = side;
+    v->n_nodes = n_nodes;
+    uint64_t s = side > 0xFFFFFFFFull ? 0xFFFFFFFFull : side;
+    v->dim[0] = v->dim[1] = v->dim[2] = (uint32_t)s;
+    v->bytes = n_nodes * 40;
+    r = c->device_alloc(&v->data, v->bytes, "xn_volume_upload_svo");
+    if (r) { delete v; return r; }
+    cudaError_t e = cudaMemcpyAsync(v->data, nodes, v->bytes, cudaMemcpyHostToDevice, c->stream);
+    uint32_t* flags = nullptr;  // [0] = bad index, [1] = has ropes
+    if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&flags), 8, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, 8, c->stream);
+    if (e == cudaSuccess) {
+        validate_nodes_kernel<<<1024, 256, 0, c->stream>>>(static_cast<const uint32_t*>(v->data), n_nodes, flags);
+        detect_ropes_kernel<<<1024, 256, 0, c->stream>>>(static_cast<const uint32_t*>(v->data), n_nodes, flags + 1);
+        e = cudaGetLastError();
+    }
+    uint32_t hf[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hf, flags, 8, cudaMemcpyDeviceToHost, c->stream);
+    if (flags) cudaFreeAsync(flags, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess || hf[0]) {
+        c->device_free(v->data, v->bytes);
+        delete v;
+        if (e != cudaSuccess) return cuda_fail(e, "xn_volume_upload_svo");
+        return fail(XN_ERR_FORMAT, "xn_volume_upload_svo: a child index is >= the node count (%llu)",
+                    (unsigned long long)n_nodes);
+    }
+    v->has_ropes = hf[1] != 0;
+    *out = reinterpret_cast<xn_volume*>(v);
+    return XN_OK;
+}
+
+XN_API int xn_volume_release(xn_volume* h) {
+    if (!h) return XN_OK;
+    Volume* v = reinterpret_cast<Volume*>(h);
+    Ctx* c = v->ctx;
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->activate();
+    cudaStreamSynchronize(c->stream);
+    c->device_free(v->data, v->bytes);
+    delete v;
+    return XN_OK;
+}
+
+XN_API int xn_volume_info_get(const xn_volume* h, xn_volume_info* info) {
+    if (!h || !info) return fail(XN_ERR_ARG, "xn_volume_info_get: NULL argument");
+    const Volume* v = reinterpret_cast<const Volume*>(h);
+    info->kind = v->kind;
+    for (int i = 0; i < 3; ++i) info->dim[i] = v->dim[i];
+    info->side = v->side;
+    info->n_nodes = v->n_nodes;
+    info->device_bytes = v->bytes;
+    info->has_ropes = v->has_ropes;
+    return XN_OK;
+}
+
+// ----------------------------------------------------------------- render ---
+
+namespace xn {
+
+int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_params* p, RenderLaunch& L) {
+    if (traversal < XN_DDA || traversal > XN_SVO_ROPE) return fail(XN_ERR_ARG, "invalid traversal %d", traversal);
+    if (traversal == XN_DDA && v->kind != XN_VOLUME_GRID)
+        return fail(XN_ERR_ARG, "traversal 'dda' requires a grid volume (tiff)");
+    if (traversal != XN_DDA && v->kind != XN_VOLUME_SVO)
+        return fail(XN_ERR_ARG, "octree traversals require an octree volume (svo)");
+    if (p->output_region.width == 0 || p->output_region.height == 0)
+        return fail(XN_ERR_ARG, "empty output region");
+    if (p->display_region.width == 0 || p->display_region.height == 0)
+        return fail(XN_ERR_ARG, "empty display region");
+    for (int i = 0; i < 3; ++i)
+        if (!(p->voxel_ratio[i] > 0.0f)) return fail(XN_ERR_ARG, "voxel ratio components must be > 0");
+    if (!(p->emission_coeff >= 0.0f)) return fail(XN_ERR_ARG, "emission coefficient must be >= 0");
+    std::memset(&L, 0, sizeof L);
+    L.traversal = traversal;
+    for (int i = 0; i < 3; ++i) {
+        L.forward[i] = cam->forward[i];
+        L.up[i] = cam->up[i];
+        L.voxel_ratio[i] = p->voxel_ratio[i];
+        // src/render/Renderer.cpp:62: translation pre-divided by the voxel ratio
+        L.translation[i] = cam->translation[i] / p->voxel_ratio[i];
+    }
+    L.aspect = (float)p->display_region.height / (float)p->display_region.width;
+    L.emission_coeff = p->emission_coeff;
+    L.out_x = p->output_region.x;
+    L.out_y = p->output_region.y;
+    L.out_w = p->output_region.width;
+    L.out_h = p->output_region.height;
+    L.disp_x = p->display_region.x;
+    L.disp_y = p->display_region.y;
+    L.disp_w = p->display_region.width;
+    L.disp_h = p->display_region.height;
+    if (v->kind == XN_VOLUME_GRID) {
+        L.grid = v->data;
+    } else {
+        L.nodes = v->data;
+    }
+    for (int i = 0; i < 3; ++i) L.dim[i] = v->dim[i];
+    return XN_OK;
+}
+
+}  // namespace xn
+
+XN_API int xn_render_device(xn_ctx* h, const xn_volume* vh, int traversal, const xn_camera* cam,
+                            const xn_params* params, void* d_rgba, float* d_emission, uint32_t* d_loads,
+                            void* stream) {
+    if (!h || !vh || !cam || !params || !d_rgba) return fail(XN_ERR_ARG, "xn_render_device: NULL argument");
+    Ctx* c = reinterpret_cast<Ctx*>(h);
+    const Volume* v = reinterpret_cast<const Volume*>(vh);
+    if (v->ctx != c) return fail(XN_ERR_ARG, "xn_render_device: volume belongs to another context");
+    RenderLaunch L;
+    int r = make_launch(v, traversal, cam, params, L);
+    if (r) return r;
+    L.d_rgba = d_rgba;
+    L.d_emission = d_emission;
+    L.d_loads = d_loads;
+    L.d_err_word = c->d_err;
+    r = c->activate();
+    if (r) return r;
+    cudaError_t e = launch_render(L, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? XN_OK : cuda_fail(e, "xn_render_device: launch");
+}
+
+XN_API int xn_render(xn_ctx* h, const xn_volume* vh, int traversal, const xn_camera* cam, const xn_params* params,
+                     uint8_t* out_rgba, float* out_emission, float* kernel_ms) {
+    if (!h || !vh || !cam || !params) return fail(XN_ERR_ARG, "xn_render: NULL argument");
+    Ctx* c = reinterpret_cast<Ctx*>(h);
+    const Volume* v = reinterpret_cast<const Volume*>(vh);
+    if (v->ctx != c) return fail(XN_ERR_ARG, "xn_render: volume belongs to another context");
+    RenderLaunch L;
+    int r = make_launch(v, traversal, cam, params, L);
+    if (r) return r;
+    std::lock_guard<std::mutex> lk(c->mu);
+    if ((r = c->activate())) return r;
+    const uint64_t npix = (uint64_t)L.out_w * L.out_h;
+    if ((r = c->ensure_buffer(c->out_rgba, npix * 4, "xn_render: output image"))) return r;
+    if (out_emission && (r = c->ensure_buffer(c->out_emission, npix * 12, "xn_render: emission buffer"))) return r;
+    L.d_rgba = c->out_rgba.ptr;
+    L.d_emission = out_emission ? static_cast<float*>(c->out_emission.ptr) : nullptr;
+    L.d_loads = nullptr;
+    L.d_err_word = c->d_err;
+    cudaError_t e = cudaMemsetAsync(c->d_err, 0, sizeof(uint32_t), c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev0, c->stream);
+    if (e == cudaSuccess) e = launch_render(L, c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->stream);
+    if (e == cudaSuccess && out_rgba)
+        e = cudaMemcpyAsync(out_rgba, c->out_rgba.ptr, npix * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && out_emission)
+        e = cudaMemcpyAsync(out_emission, c->out_emission.ptr, npix * 12, cudaMemcpyDeviceToHost, c->stream);
+    uint32_t err_bits = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&err_bits, c->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "xn_render");
+    if (kernel_ms) {
+        e = cudaEventElapsedTime(kernel_ms, c->ev0, c->ev1);
+        if (e != cudaSuccess) return cuda_fail(e, "xn_render: event timing");
+    }
+    if (err_bits) return fail(XN_ERR_RAY_LIMIT, "xn_render: a ray hit an iteration or stack limit (bits 0x%x)", err_bits);
+    return XN_OK;
+}
+
+XN_API int xn_ray_errors(xn_ctx* h, uint32_t* bits, int reset) {
+    if (!h || !bits) return fail(XN_ERR_ARG, "xn_ray_errors: NULL argument");
+    Ctx* c = reinterpret_cast<Ctx*>(h);
+    std::lock_guard<std::mutex> lk(c->mu);
+    int r = c->activate();
+    if (r) return r;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(bits, c->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && reset) e = cudaMemset(c->d_err, 0, sizeof(uint32_t));
+    return e == cudaSuccess ? XN_OK : cuda_fail(e, "xn_ray_errors");
+}
+
+XN_API void xn_free(void* p) { std::free(p); }

@@ -1,0 +1,149 @@
+"""Seeded synthetic volumes standing in for the reference's datasets.
+
+The reference renders a CT scan of the Stanford bunny (512x361x512) and TNG
+gas fields (1024^3, 2048^3) prepared by tools/make-bunny-volume.py and
+tools/make-tng-volume.py; none of that data is available, so these generators
+produce volumes of the same shapes and value distributions.  All voxels are
+RGBA8 with alpha 255 (as tools/make-bunny-volume.py:48 writes), "zeroed" means
+RGB = 0, and arrays are laid out (dz, dy, dx, 4), x fastest, like
+src/model/Grid.h:50-52.
+
+Randomness comes from integer hashes of voxel coordinates and a seed, so a
+volume is the same whichever torch device evaluates it (up to float rounding in
+the smooth noise).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+_M32 = 0xFFFFFFFF
+
+
+def _hash32(a: torch.Tensor) -> torch.Tensor:
+    """Thomas Wang's 32-bit integer hash on int64 tensors holding u32 values."""
+    a = ((a ^ 61) ^ (a >> 16)) & _M32
+    a = (a + (a << 3)) & _M32
+    a = a ^ (a >> 4)
+    a = (a * 0x27D4EB2D) & _M32
+    a = a ^ (a >> 15)
+    return a
+
+
+def _uniform(x, y, z, seed: int, salt: int) -> torch.Tensor:
+    """Uniform [0, 1) per integer coordinate."""
+    h = _hash32((x * 73856093) & _M32)
+    h = _hash32(h ^ ((y * 19349663) & _M32))
+    h = _hash32(h ^ ((z * 83492791) & _M32))
+    h = _hash32(h ^ ((seed * 2654435761 + salt * 40503) & _M32))
+    return h.to(torch.float64) / 4294967296.0
+
+
+def _value_noise(xf, yf, zf, cell: float, seed: int, salt: int) -> torch.Tensor:
+    """Trilinear value noise in [-1, 1] with lattice spacing `cell` voxels."""
+    gx, gy, gz = xf / cell, yf / cell, zf / cell
+    ix, iy, iz = torch.floor(gx), torch.floor(gy), torch.floor(gz)
+    fx, fy, fz = gx - ix, gy - iy, gz - iz
+    # smoothstep weights
+    fx, fy, fz = fx * fx * (3 - 2 * fx), fy * fy * (3 - 2 * fy), fz * fz * (3 - 2 * fz)
+    ix, iy, iz = ix.to(torch.int64), iy.to(torch.int64), iz.to(torch.int64)
+    out = torch.zeros_like(xf)
+    for dx in (0, 1):
+        wx = fx if dx else 1 - fx
+        for dy in (0, 1):
+            wy = fy if dy else 1 - fy
+            for dz in (0, 1):
+                wz = fz if dz else 1 - fz
+                v = _uniform(ix + dx, iy + dy, iz + dz, seed, salt) * 2 - 1
+                out += wx * wy * wz * v
+    return out
+
+
+def _device(device):
+    if device is not None:
+        return torch.device(device)
+    return torch.device("cuda") if torch.cuda.is_available() else torch.device("cpu")
+
+
+def blobs(n: int = 128, seed: int = 0, count: int = 16) -> np.ndarray:
+    """16 isotropic Gaussian blobs in an n^3 grid (the 128^3 DDA workload).
+
+    Centres uniform in [0.2, 0.8]^3 of the extent, sigma uniform in
+    [0.03, 0.1] of the extent, per-blob RGB uniform in [0, 255]; the colours
+    are summed and clamped to 255 per channel, and voxels whose largest channel
+    is below 8 are zeroed (about 80% of the volume is empty)."""
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(0.2, 0.8, (count, 3)) * n
+    sigmas = rng.uniform(0.03, 0.1, count) * n
+    colours = rng.integers(0, 256, (count, 3)).astype(np.float64)
+    c = (np.arange(n) + 0.5)
+    acc = np.zeros((n, n, n, 3), np.float64)
+    for k in range(count):
+        gz = np.exp(-((c - centres[k, 2]) ** 2) / (2 * sigmas[k] ** 2))
+        gy = np.exp(-((c - centres[k, 1]) ** 2) / (2 * sigmas[k] ** 2))
+        gx = np.exp(-((c - centres[k, 0]) ** 2) / (2 * sigmas[k] ** 2))
+        w = gz[:, None, None] * gy[None, :, None] * gx[None, None, :]
+        acc += w[..., None] * colours[k]
+    rgb = np.minimum(np.floor(acc), 255).astype(np.uint8)
+    rgb[rgb.max(axis=3) < 8] = 0
+    out = np.empty((n, n, n, 4), np.uint8)
+    out[..., :3] = rgb
+    out[..., 3] = 255
+    return out
+
+
+def ct_shell(dx: int = 512, dy: int = 361, dz: int = 512, seed: int = 1, device=None) -> np.ndarray:
+    """CT-scan-shaped volume (the 512x361x512 bunny stand-in).
+
+    A closed ellipsoidal shell with semi-axes 0.40/0.35/0.30 of the largest
+    extent and a thickness of 3-6 voxels, its radius perturbed by 3-octave
+    value noise of amplitude 0.05; the interior holds gray N(90, 20) clamped to
+    [1, 255] at 20% of its voxels; the background is 0."""
+    dev = _device(device)
+    ext = float(max(dx, dy, dz))
+    a, b, c = 0.40 * ext, 0.35 * ext, 0.30 * ext
+    cx, cy, cz = dx / 2.0, dy / 2.0, dz / 2.0
+    mean_axis = (a + b + c) / 3.0
+    out = np.empty((dz, dy, dx, 4), np.uint8)
+    slab = max(1, (1 << 24) // (dx * dy))
+    ys = torch.arange(dy, device=dev, dtype=torch.int64)
+    xs = torch.arange(dx, device=dev, dtype=torch.int64)
+    for z0 in range(0, dz, slab):
+        z1 = min(dz, z0 + slab)
+        zs = torch.arange(z0, z1, device=dev, dtype=torch.int64)
+        Z, Y, X = torch.meshgrid(zs, ys, xs, indexing="ij")
+        xf, yf, zf = X.double() + 0.5, Y.double() + 0.5, Z.double() + 0.5
+        rho = torch.sqrt(((xf - cx) / a) ** 2 + ((yf - cy) / b) ** 2 + ((zf - cz) / c) ** 2)
+        noise = (_value_noise(xf, yf, zf, ext / 8, seed, 1) + 0.5 * _value_noise(xf, yf, zf, ext / 16, seed, 2)
+                 + 0.25 * _value_noise(xf, yf, zf, ext / 32, seed, 3)) / 1.75
+        rho = rho * (1.0 + 0.05 * noise)
+        thick = 3.0 + 3.0 * (0.5 + 0.5 * _value_noise(xf, yf, zf, ext / 12, seed, 4))
+        dist = (rho - 1.0) * mean_axis  # signed distance in voxels, approximately
+        shell = dist.abs() <= thick / 2
+        inner = dist < -thick / 2
+        u1 = _uniform(X, Y, Z, seed, 5)
+        u2 = _uniform(X, Y, Z, seed, 6).clamp_min(1e-12)
+        u3 = _uniform(X, Y, Z, seed, 7)
+        gauss = torch.sqrt(-2.0 * torch.log(u2)) * torch.cos(2 * math.pi * u3)
+        gray = (90.0 + 20.0 * gauss).round().clamp(1, 255)
+        shell_val = (200.0 + 40.0 * _value_noise(xf, yf, zf, 4.0, seed, 8)).round().clamp(1, 255)
+        v = torch.zeros_like(xf)
+        v = torch.where(inner & (u1 < 0.2), gray, v)
+        v = torch.where(shell, shell_val, v)
+        g8 = v.to(torch.uint8)
+        blk = torch.stack([g8, g8, g8, torch.full_like(g8, 255)], dim=-1)
+        out[z0:z1] = blk.cpu().numpy()
+    return out
+
+
+def random_grid(dz: int, dy: int, dx: int, seed: int = 0, density: float = 0.3, levels: int = 256) -> np.ndarray:
+    """Small random test grid: `density` of voxels non-zero, alpha 255."""
+    rng = np.random.default_rng(seed)
+    g = np.zeros((dz, dy, dx, 4), np.uint8)
+    m = rng.random((dz, dy, dx)) < density
+    vals = rng.integers(0, levels, (int(m.sum()), 3)) * (255 // max(1, levels - 1))
+    g[m, :3] = np.minimum(vals, 255).astype(np.uint8)
+    g[..., 3] = 255
+    return g
