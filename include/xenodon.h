@@ -180,4 +180,18 @@ XN_API void xn_free(void* p);
 XN_API int xn_svo_load(const char* path, uint32_t** nodes_out, uint64_t* n_nodes, uint64_t* side);
 XN_API int xn_svo_save(const char* path, const uint32_t* nodes, uint64_t n_nodes, uint64_t side);
 
+/* Grid::load_tiff (src/model/Grid.cpp:27-79): a stacked TIFF, one page per z
+ * slice, read the way TIFFReadRGBAImage hands it to the reference (rows
+ * bottom-up, gray expanded to RGB, alpha 255 when absent, unassociated alpha
+ * premultiplied).  Uncompressed 8-bit gray/RGB/RGBA, strips or tiles, classic
+ * TIFF or BigTIFF.  *rgba_out is malloc'd (dims[0]*dims[1]*dims[2]*4 bytes,
+ * x fastest); free it with xn_free. */
+XN_API int xn_tiff_load(const char* path, uint8_t** rgba_out, uint32_t dims_out[3]);
+/* Writes a grid as an uncompressed RGBA BigTIFF that xn_tiff_load (and
+ * libtiff's TIFFReadRGBAImage) reads back unchanged. */
+XN_API int xn_tiff_save(const char* path, const uint8_t* rgba, uint32_t dx, uint32_t dy, uint32_t dz);
+/* HeadlessDisplay::save's PNG output (src/backend/headless/HeadlessDisplay.cpp:80-85):
+ * width*height RGBA8 pixels, row-major, top row first. */
+XN_API int xn_png_save(const char* path, const uint8_t* rgba, uint32_t width, uint32_t height);
+
 #endif

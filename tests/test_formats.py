@@ -1,0 +1,196 @@
+"""Host file formats through the C ABI (CPU only): stacked TIFF as
+TIFFReadRGBAImage hands it to the reference (src/model/Grid.cpp:27-79) and
+PNG frames."""
+from __future__ import annotations
+
+import struct
+import zlib
+
+import numpy as np
+import pytest
+
+
+def _classic_tiff(pages, photometric, spp, extra=None, big_endian=False, tile=None):
+    """Minimal independent TIFF writer: pages is a list of uint8 (h, w, spp)."""
+    e = ">" if big_endian else "<"
+    out = bytearray(b"MM" if big_endian else b"II")
+    out += struct.pack(e + "HI", 42, 8)
+    offsets = []
+    for i, img in enumerate(pages):
+        h, w = img.shape[:2]
+        entries = []
+        data_parts = []
+        if tile:
+            tw, th = tile
+            tx, ty = -(-w // tw), -(-h // th)
+            for j in range(ty):
+                for k in range(tx):
+                    t = np.zeros((th, tw, spp), np.uint8)
+                    blk = img[j * th:(j + 1) * th, k * tw:(k + 1) * tw]
+                    t[:blk.shape[0], :blk.shape[1]] = blk
+                    data_parts.append(t.tobytes())
+        else:
+            data_parts.append(img.tobytes())
+        n_entries = 10 + (1 if extra is not None else 0) + (1 if tile else 0)
+        ifd_off = len(out)
+        after_ifd = ifd_off + 2 + 12 * n_entries + 4
+        bps_off = after_ifd
+        offs_off = bps_off + 2 * spp
+        cnt_off = offs_off + 4 * len(data_parts)
+        data_off = cnt_off + 4 * len(data_parts)
+        poffs, pcnts = [], []
+        p = data_off
+        for d in data_parts:
+            poffs.append(p)
+            pcnts.append(len(d))
+            p += len(d)
+        next_off = p if i + 1 < len(pages) else 0
+
+        def ent(tag, typ, count, value):
+            if typ == 3 and count == 1:
+                return struct.pack(e + "HHIHH", tag, typ, count, value, 0)
+            return struct.pack(e + "HHII", tag, typ, count, value)
+
+        entries.append(ent(256, 4, 1, w))
+        entries.append(ent(257, 4, 1, h))
+        entries.append(ent(258, 3, spp, bps_off) if spp > 2 else ent(258, 3, 1, 8))
+        entries.append(ent(259, 3, 1, 1))
+        entries.append(ent(262, 3, 1, photometric))
+        entries.append(ent(324 if tile else 273, 4, len(poffs), offs_off if len(poffs) > 1 else poffs[0]))
+        entries.append(ent(277, 3, 1, spp))
+        if tile:
+            entries.append(ent(322, 3, 1, tile[0]))
+            entries.append(ent(323, 3, 1, tile[1]))
+        else:
+            entries.append(ent(278, 4, 1, h))
+        entries.append(ent(325 if tile else 279, 4, len(pcnts), cnt_off if len(pcnts) > 1 else pcnts[0]))
+        entries.append(ent(284, 3, 1, 1))
+        if extra is not None:
+            entries.append(ent(338, 3, 1, extra))
+        entries.sort(key=lambda b: struct.unpack(e + "H", b[:2])[0])
+        assert len(entries) == n_entries
+        out += struct.pack(e + "H", n_entries) + b"".join(entries) + struct.pack(e + "I", next_off)
+        out += struct.pack(e + "H" * spp, *([8] * spp))
+        out += struct.pack(e + "I" * len(poffs), *poffs)
+        out += struct.pack(e + "I" * len(pcnts), *pcnts)
+        for d in data_parts:
+            out += d
+        offsets.append(ifd_off)
+    return bytes(out)
+
+
+def test_tiff_gray_pages_are_bottom_up_rgb(built_library, tmp_path):
+    import xenodon_gb300 as xg
+    rng = np.random.default_rng(0)
+    pages = [rng.integers(0, 256, (5, 7, 1)).astype(np.uint8) for _ in range(3)]
+    p = tmp_path / "g.tif"
+    p.write_bytes(_classic_tiff(pages, photometric=1, spp=1))
+    g = xg.tiff_load(p)
+    assert g.shape == (3, 5, 7, 4)
+    for z, img in enumerate(pages):
+        for y in range(5):
+            assert np.array_equal(g[z, y, :, 0], img[4 - y, :, 0])  # grid row y = image row h-1-y
+    assert np.array_equal(g[..., 0], g[..., 1]) and np.array_equal(g[..., 0], g[..., 2])
+    assert np.all(g[..., 3] == 255)
+
+
+@pytest.mark.parametrize("big_endian", [False, True])
+def test_tiff_rgb_and_tiles(built_library, tmp_path, big_endian):
+    import xenodon_gb300 as xg
+    rng = np.random.default_rng(1)
+    pages = [rng.integers(0, 256, (9, 11, 3)).astype(np.uint8) for _ in range(2)]
+    for tile in (None, (16, 16)):
+        p = tmp_path / "rgb.tif"
+        p.write_bytes(_classic_tiff(pages, photometric=2, spp=3, big_endian=big_endian, tile=tile))
+        g = xg.tiff_load(p)
+        assert g.shape == (2, 9, 11, 4)
+        for z in range(2):
+            assert np.array_equal(g[z, :, :, :3], pages[z][::-1])
+        assert np.all(g[..., 3] == 255)
+
+
+def test_tiff_rgba_alpha_handling(built_library, tmp_path):
+    import xenodon_gb300 as xg
+    rng = np.random.default_rng(2)
+    img = rng.integers(0, 256, (4, 6, 4)).astype(np.uint8)
+    # associated alpha: kept as stored
+    p = tmp_path / "a.tif"
+    p.write_bytes(_classic_tiff([img], photometric=2, spp=4, extra=1))
+    assert np.array_equal(xg.tiff_load(p)[0], img[::-1])
+    # unassociated alpha: premultiplied as libtiff's RGBA interface does
+    p.write_bytes(_classic_tiff([img], photometric=2, spp=4, extra=2))
+    got = xg.tiff_load(p)[0]
+    a = img[..., 3:4].astype(np.uint32)
+    exp = img.copy()
+    exp[..., :3] = ((img[..., :3].astype(np.uint32) * a + 127) // 255).astype(np.uint8)
+    assert np.array_equal(got, exp[::-1])
+
+
+def test_tiff_roundtrip_of_own_writer(built_library, tmp_path):
+    import xenodon_gb300 as xg
+    from xenodon_gb300 import volumes
+    g = volumes.random_grid(6, 5, 9, seed=3)  # alpha 255: unchanged by premultiplication
+    xg.tiff_save(tmp_path / "v.tif", g)
+    assert np.array_equal(xg.tiff_load(tmp_path / "v.tif"), g)
+
+
+@pytest.mark.parametrize("data,msg", [
+    (b"XX*\x00" + b"\0" * 20, "not a TIFF"),
+    (b"II*\x00\x08\x00\x00\x00\x05", "truncated directory"),
+])
+def test_tiff_malformed(built_library, tmp_path, data, msg):
+    import xenodon_gb300 as xg
+    p = tmp_path / "bad.tif"
+    p.write_bytes(data)
+    with pytest.raises(xg.XenodonError) as e:
+        xg.tiff_load(p)
+    assert msg in str(e.value)
+
+
+def test_tiff_missing_file(built_library, tmp_path):
+    import xenodon_gb300 as xg
+    with pytest.raises(xg.XenodonError) as e:
+        xg.tiff_load(tmp_path / "nope.tif")
+    assert "Failed to open" in str(e.value)
+
+
+def test_tiff_layer_size_check_follows_reference(built_library, tmp_path):
+    # Grid.cpp:47 rejects a layer only when width AND height differ
+    import xenodon_gb300 as xg
+    a = np.zeros((4, 5, 1), np.uint8)
+    b = np.zeros((3, 6, 1), np.uint8)
+    p = tmp_path / "d.tif"
+    p.write_bytes(_classic_tiff([a, b], photometric=1, spp=1))
+    with pytest.raises(xg.XenodonError) as e:
+        xg.tiff_load(p)
+    assert "differ from previous dimensions" in str(e.value)
+    c = np.zeros((4, 6, 1), np.uint8)  # same height: accepted like the reference
+    p.write_bytes(_classic_tiff([a, c], photometric=1, spp=1))
+    assert xg.tiff_load(p).shape == (2, 4, 5, 4)
+
+
+def _png_decode(data: bytes) -> np.ndarray:
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    pos, idat = 8, b""
+    while pos < len(data):
+        n, = struct.unpack(">I", data[pos:pos + 4])
+        t, c = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + n]
+        crc, = struct.unpack(">I", data[pos + 8 + n:pos + 12 + n])
+        assert crc == zlib.crc32(t + c) & 0xFFFFFFFF
+        if t == b"IHDR":
+            w, h, depth, ctype = struct.unpack(">IIBB", c[:10])
+            assert (depth, ctype) == (8, 6)
+        elif t == b"IDAT":
+            idat += c
+        pos += 12 + n
+    raw = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(h, w * 4 + 1)
+    assert np.all(raw[:, 0] == 0)
+    return raw[:, 1:].reshape(h, w, 4)
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (33, 47), (300, 251)])
+def test_png_decodes_to_the_pixels(built_library, tmp_path, shape):
+    import xenodon_gb300 as xg
+    img = np.random.default_rng(4).integers(0, 256, shape + (4,)).astype(np.uint8)
+    xg.png_save(tmp_path / "f.png", img)
+    assert np.array_equal(_png_decode((tmp_path / "f.png").read_bytes()), img)

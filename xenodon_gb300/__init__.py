@@ -32,7 +32,7 @@ EXPORTS = (
     "xn_create", "xn_destroy", "xn_last_error", "xn_abi_version", "xn_ctx_memory",
     "xn_volume_upload_grid", "xn_volume_upload_svo", "xn_volume_release", "xn_volume_info_get",
     "xn_render", "xn_render_device", "xn_ray_errors", "xn_build_svo", "xn_free",
-    "xn_svo_load", "xn_svo_save",
+    "xn_svo_load", "xn_svo_save", "xn_tiff_load", "xn_tiff_save", "xn_png_save",
 )
 
 
@@ -99,6 +99,9 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "xn_free": (None, [vp]),
         "xn_svo_load": (i32, [ctypes.c_char_p, P(P(u32)), P(u64), P(u64)]),
         "xn_svo_save": (i32, [ctypes.c_char_p, vp, u64, u64]),
+        "xn_tiff_load": (i32, [ctypes.c_char_p, P(P(ctypes.c_uint8)), P(u32 * 3)]),
+        "xn_tiff_save": (i32, [ctypes.c_char_p, vp, u32, u32, u32]),
+        "xn_png_save": (i32, [ctypes.c_char_p, vp, u32, u32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(l, name)
@@ -214,10 +217,18 @@ class Context:
         return Volume(self, h)
 
     def render(self, vol: Volume, traversal, camera: Camera, params: Params, emission: bool = False,
-               allow_ray_limit: bool = False):
-        """Render to host memory.  Returns (rgba (h, w, 4) u8, emission (h, w, 3) f32 or None, kernel_ms)."""
+               allow_ray_limit: bool = False, out: np.ndarray | None = None):
+        """Render to host memory.  Returns (rgba (h, w, 4) u8, emission (h, w, 3) f32 or None, kernel_ms).
+
+        `out`, when given, is a C-contiguous uint8 (h, w, 4) host array (pinned
+        memory makes the copy asynchronous-capable and faster)."""
         w, h = params.output_region.width, params.output_region.height
-        rgba = np.empty((h, w, 4), np.uint8)
+        if out is not None:
+            if out.dtype != np.uint8 or out.shape != (h, w, 4) or not out.flags["C_CONTIGUOUS"]:
+                raise ValueError("out must be a C-contiguous uint8 array of shape (h, w, 4)")
+            rgba = out
+        else:
+            rgba = np.empty((h, w, 4), np.uint8)
         em = np.empty((h, w, 3), np.float32) if emission else None
         ms = ctypes.c_float()
         r = self.lib.xn_render(self.handle, vol.handle, _traversal(traversal), ctypes.byref(camera),
@@ -270,3 +281,27 @@ def svo_load(path) -> tuple[np.ndarray, int]:
 def svo_save(path, nodes: np.ndarray, side: int) -> None:
     n = np.ascontiguousarray(nodes, dtype=np.uint32).reshape(-1, 10)
     _check(load_library().xn_svo_save(str(path).encode(), n.ctypes.data, n.shape[0], int(side)))
+
+
+def tiff_load(path) -> np.ndarray:
+    """Stacked TIFF -> uint8 (dz, dy, dx, 4), as the reference's Grid::load_tiff sees it."""
+    lib = load_library()
+    out = ctypes.POINTER(ctypes.c_uint8)()
+    dims = (ctypes.c_uint32 * 3)()
+    _check(lib.xn_tiff_load(str(path).encode(), ctypes.byref(out), ctypes.byref(dims)))
+    try:
+        n = dims[0] * dims[1] * dims[2] * 4
+        arr = np.ctypeslib.as_array(out, shape=(n,)).copy().reshape(dims[2], dims[1], dims[0], 4)
+    finally:
+        lib.xn_free(out)
+    return arr
+
+
+def tiff_save(path, grid: np.ndarray) -> None:
+    g = np.ascontiguousarray(grid, dtype=np.uint8)
+    _check(load_library().xn_tiff_save(str(path).encode(), g.ctypes.data, g.shape[2], g.shape[1], g.shape[0]))
+
+
+def png_save(path, rgba: np.ndarray) -> None:
+    a = np.ascontiguousarray(rgba, dtype=np.uint8)
+    _check(load_library().xn_png_save(str(path).encode(), a.ctypes.data, a.shape[1], a.shape[0]))

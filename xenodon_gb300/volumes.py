@@ -41,26 +41,6 @@ def _uniform(x, y, z, seed: int, salt: int) -> torch.Tensor:
     return h.to(torch.float64) / 4294967296.0
 
 
-def _value_noise(xf, yf, zf, cell: float, seed: int, salt: int) -> torch.Tensor:
-    """Trilinear value noise in [-1, 1] with lattice spacing `cell` voxels."""
-    gx, gy, gz = xf / cell, yf / cell, zf / cell
-    ix, iy, iz = torch.floor(gx), torch.floor(gy), torch.floor(gz)
-    fx, fy, fz = gx - ix, gy - iy, gz - iz
-    # smoothstep weights
-    fx, fy, fz = fx * fx * (3 - 2 * fx), fy * fy * (3 - 2 * fy), fz * fz * (3 - 2 * fz)
-    ix, iy, iz = ix.to(torch.int64), iy.to(torch.int64), iz.to(torch.int64)
-    out = torch.zeros_like(xf)
-    for dx in (0, 1):
-        wx = fx if dx else 1 - fx
-        for dy in (0, 1):
-            wy = fy if dy else 1 - fy
-            for dz in (0, 1):
-                wz = fz if dz else 1 - fz
-                v = _uniform(ix + dx, iy + dy, iz + dz, seed, salt) * 2 - 1
-                out += wx * wy * wz * v
-    return out
-
-
 def _device(device):
     if device is not None:
         return torch.device(device)
@@ -106,35 +86,69 @@ def ct_shell(dx: int = 512, dy: int = 361, dz: int = 512, seed: int = 1, device=
     a, b, c = 0.40 * ext, 0.35 * ext, 0.30 * ext
     cx, cy, cz = dx / 2.0, dy / 2.0, dz / 2.0
     mean_axis = (a + b + c) / 3.0
+    f32 = torch.float32
+    xs = torch.arange(dx, device=dev, dtype=f32) + 0.5
+    ys = torch.arange(dy, device=dev, dtype=f32) + 0.5
+    # smooth fields over the whole volume are evaluated slab by slab with the
+    # lattice origin fixed at 0, so slabs join seamlessly
     out = np.empty((dz, dy, dx, 4), np.uint8)
-    slab = max(1, (1 << 24) // (dx * dy))
-    ys = torch.arange(dy, device=dev, dtype=torch.int64)
-    xs = torch.arange(dx, device=dev, dtype=torch.int64)
+    slab = max(1, (1 << 23) // (dx * dy))
+    xi = torch.arange(dx, device=dev, dtype=torch.int64)[None, None, :]
+    yi = torch.arange(dy, device=dev, dtype=torch.int64)[None, :, None]
     for z0 in range(0, dz, slab):
         z1 = min(dz, z0 + slab)
-        zs = torch.arange(z0, z1, device=dev, dtype=torch.int64)
-        Z, Y, X = torch.meshgrid(zs, ys, xs, indexing="ij")
-        xf, yf, zf = X.double() + 0.5, Y.double() + 0.5, Z.double() + 0.5
-        rho = torch.sqrt(((xf - cx) / a) ** 2 + ((yf - cy) / b) ** 2 + ((zf - cz) / c) ** 2)
-        noise = (_value_noise(xf, yf, zf, ext / 8, seed, 1) + 0.5 * _value_noise(xf, yf, zf, ext / 16, seed, 2)
-                 + 0.25 * _value_noise(xf, yf, zf, ext / 32, seed, 3)) / 1.75
+        zs = torch.arange(z0, z1, device=dev, dtype=f32) + 0.5
+        X, Y, Z = ((xs - cx) / a)[None, None, :], ((ys - cy) / b)[None, :, None], ((zs - cz) / c)[:, None, None]
+        rho = torch.sqrt(X * X + Y * Y + Z * Z)
+        noise = (_noise_fixed(xs, ys, zs, ext / 8, seed, 1) + 0.5 * _noise_fixed(xs, ys, zs, ext / 16, seed, 2)
+                 + 0.25 * _noise_fixed(xs, ys, zs, ext / 32, seed, 3)) / 1.75
         rho = rho * (1.0 + 0.05 * noise)
-        thick = 3.0 + 3.0 * (0.5 + 0.5 * _value_noise(xf, yf, zf, ext / 12, seed, 4))
+        thick = 3.0 + 3.0 * (0.5 + 0.5 * _noise_fixed(xs, ys, zs, ext / 12, seed, 4))
         dist = (rho - 1.0) * mean_axis  # signed distance in voxels, approximately
         shell = dist.abs() <= thick / 2
         inner = dist < -thick / 2
-        u1 = _uniform(X, Y, Z, seed, 5)
-        u2 = _uniform(X, Y, Z, seed, 6).clamp_min(1e-12)
-        u3 = _uniform(X, Y, Z, seed, 7)
+        zi = torch.arange(z0, z1, device=dev, dtype=torch.int64)[:, None, None]
+        lin = (xi + dx * (yi + dy * zi)) & _M32
+        h1 = _hash32(lin ^ ((seed * 0x9E3779B1 + 5) & _M32))
+        h2 = _hash32(h1 ^ 0x68E31DA4)
+        h3 = _hash32(h2 ^ 0x1B56C4E9)
+        u1 = h1.to(f32) / 4294967296.0
+        u2 = (h2.to(f32) + 1.0) / 4294967297.0
+        u3 = h3.to(f32) / 4294967296.0
         gauss = torch.sqrt(-2.0 * torch.log(u2)) * torch.cos(2 * math.pi * u3)
         gray = (90.0 + 20.0 * gauss).round().clamp(1, 255)
-        shell_val = (200.0 + 40.0 * _value_noise(xf, yf, zf, 4.0, seed, 8)).round().clamp(1, 255)
-        v = torch.zeros_like(xf)
-        v = torch.where(inner & (u1 < 0.2), gray, v)
+        shell_val = (200.0 + 40.0 * _noise_fixed(xs, ys, zs, 4.0, seed, 8)).round().clamp(1, 255)
+        v = torch.where(inner & (u1 < 0.2), gray, torch.zeros((), device=dev, dtype=f32))
         v = torch.where(shell, shell_val, v)
         g8 = v.to(torch.uint8)
         blk = torch.stack([g8, g8, g8, torch.full_like(g8, 255)], dim=-1)
         out[z0:z1] = blk.cpu().numpy()
+    return out
+
+
+def _noise_fixed(xs, ys, zs, cell: float, seed: int, salt: int) -> torch.Tensor:
+    """Value noise whose lattice is anchored at the origin of the volume."""
+    dev = xs.device
+    gx, gy, gz = xs / cell, ys / cell, zs / cell
+    ix, iy, iz = torch.floor(gx), torch.floor(gy), torch.floor(gz)
+    fx, fy, fz = gx - ix, gy - iy, gz - iz
+    fx, fy, fz = fx * fx * (3 - 2 * fx), fy * fy * (3 - 2 * fy), fz * fz * (3 - 2 * fz)
+    ix, iy, iz = ix.to(torch.int64), iy.to(torch.int64), iz.to(torch.int64)
+    lz = torch.arange(int(iz.min()), int(iz.max()) + 2, device=dev, dtype=torch.int64)
+    ly = torch.arange(0, int(iy.max()) + 2, device=dev, dtype=torch.int64)
+    lx = torch.arange(0, int(ix.max()) + 2, device=dev, dtype=torch.int64)
+    lat = (_uniform(lx[None, None, :], ly[None, :, None], lz[:, None, None], seed, salt) * 2 - 1).to(torch.float32)
+    iz = iz - int(lz[0])
+    out = None
+    for dz in (0, 1):
+        wz = (fz if dz else 1 - fz)[:, None, None]
+        for dy in (0, 1):
+            wy = (fy if dy else 1 - fy)[None, :, None]
+            for dx in (0, 1):
+                wx = (fx if dx else 1 - fx)[None, None, :]
+                v = lat[(iz + dz)[:, None, None], (iy + dy)[None, :, None], (ix + dx)[None, None, :]]
+                term = v * (wz * wy * wx)
+                out = term if out is None else out + term
     return out
 
 
