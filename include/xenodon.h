@@ -173,6 +173,26 @@ XN_API int xn_build_svo(xn_ctx* ctx, const uint8_t* rgba, uint32_t dx, uint32_t 
                         xn_build_stats* stats);
 XN_API void xn_free(void* p);
 
+/* No counterpart in the reference.  The same octree build as xn_build_svo, for
+ * callers that cannot allocate device memory: code that runs inside another
+ * framework's memory pool or under a fixed HBM budget, and host loops that must
+ * not take the device-wide synchronisation cudaMalloc/cudaFree can cause.  It
+ * allocates nothing: the grid (d_rgba: dx*dy*dz packed RGBA8 texels, x fastest,
+ * 4-byte aligned) and the node buffer (d_nodes: node_capacity nodes of 10 u32,
+ * 8-byte aligned) are the caller's device memory, and all scratch comes from one
+ * fixed 32 MiB device array that every GPU loading the library holds until the
+ * process exits.  A grid whose build needs more scratch than that (about 2
+ * million voxels for sparse or rope trees, fewer for DAGs) is rejected with
+ * XN_ERR_BUDGET before anything runs; a node buffer that is too small is rejected
+ * with XN_ERR_ARG and stats->n_nodes set to the size needed.  Work is queued on
+ * `stream` (a cudaStream_t of the current device) and the call returns once it is
+ * done.  The first call on a device looks up the scratch array's device address,
+ * so make that first call before any stream capture.  Every call reuses the
+ * same array and clears what it needs; calls that overlap on the GPU race. */
+XN_API int xn_build_svo_static(const uint32_t* d_rgba, uint32_t dx, uint32_t dy, uint32_t dz, int type,
+                               int heuristic, double threshold, uint32_t* d_nodes, uint64_t node_capacity,
+                               xn_build_stats* stats, void* stream);
+
 /* --------------------------------------------------------- file formats --- */
 
 /* Octree::load_svo / save_svo (src/model/Octree.cpp:50-114): "XNDN-SVO", u64

@@ -31,7 +31,7 @@ XN_ERR_BUDGET, XN_ERR_RAY_LIMIT, XN_ERR_IO, XN_ERR_STATE = -5, -6, -7, -8
 EXPORTS = (
     "xn_create", "xn_destroy", "xn_last_error", "xn_abi_version", "xn_ctx_memory",
     "xn_volume_upload_grid", "xn_volume_upload_svo", "xn_volume_release", "xn_volume_info_get",
-    "xn_render", "xn_render_device", "xn_ray_errors", "xn_build_svo", "xn_free",
+    "xn_render", "xn_render_device", "xn_ray_errors", "xn_build_svo", "xn_build_svo_static", "xn_free",
     "xn_svo_load", "xn_svo_save", "xn_tiff_load", "xn_tiff_save", "xn_png_save",
 )
 
@@ -96,6 +96,7 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "xn_render_device": (i32, [vp, vp, i32, P(Camera), P(Params), vp, vp, vp, vp]),
         "xn_ray_errors": (i32, [vp, P(u32), i32]),
         "xn_build_svo": (i32, [vp, vp, u32, u32, u32, i32, i32, ctypes.c_double, P(P(u32)), P(BuildStats)]),
+        "xn_build_svo_static": (i32, [vp, u32, u32, u32, i32, i32, ctypes.c_double, vp, u64, P(BuildStats), vp]),
         "xn_free": (None, [vp]),
         "xn_svo_load": (i32, [ctypes.c_char_p, P(P(u32)), P(u64), P(u64)]),
         "xn_svo_save": (i32, [ctypes.c_char_p, vp, u64, u64]),

@@ -1094,3 +1094,377 @@ XN_API int xn_build_svo(xn_ctx* h, const uint8_t* rgba, uint32_t dx, uint32_t dy
     *nodes_out = host;
     return XN_OK;
 }
+
+// --------------------------------------------------- allocation-free build ---
+//
+// xn_build_svo_static: the octree build for callers that cannot call
+// cudaMalloc -- code running inside another framework's memory pool or HBM
+// budget, or host loops that must not take the device-wide synchronisation a
+// cudaMalloc/cudaFree can imply.  The caller passes the grid (device memory)
+// and the node buffer (device memory); all scratch comes from one fixed
+// file-scope device array of XN_STATIC_SCRATCH_BYTES that every GPU loading
+// this library holds until the process exits.  Calls share that array and
+// leave their contents in it: whatever must start at zero is cleared by each
+// call, and calls that overlap on the GPU (two streams, two threads) race.
+// The same kernels as xn_build_svo run in the same order; only the source of
+// scratch differs.
+
+#define XN_STATIC_SCRATCH_BYTES (32ull << 20)
+
+static __device__ __align__(256) unsigned char xn_static_build_scratch[XN_STATIC_SCRATCH_BYTES];
+
+namespace xn {
+namespace {
+
+constexpr int STATIC_MAX_DEVICES = 64;
+std::mutex g_static_mu;
+void* g_static_scratch[STATIC_MAX_DEVICES];
+
+// Device address of the scratch array on the current device.  The first call
+// on a device looks it up with cudaGetSymbolAddress (host code must not use
+// the array's name as an address).
+int static_scratch_address(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "xn_build_svo_static: cudaGetDevice");
+    if (dev < 0 || dev >= STATIC_MAX_DEVICES)
+        return fail(XN_ERR_ARG, "xn_build_svo_static: device %d is beyond the %d supported", dev, STATIC_MAX_DEVICES);
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    if (!g_static_scratch[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, xn_static_build_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "xn_build_svo_static: cudaGetSymbolAddress");
+        g_static_scratch[dev] = p;
+    }
+    *out = g_static_scratch[dev];
+    return XN_OK;
+}
+
+// Bump allocation inside the scratch array; with base == nullptr it only
+// measures.
+struct Arena {
+    unsigned char* base;
+    uint64_t cap;
+    uint64_t used = 0;
+    bool overflow = false;
+    template <class T>
+    T* take(uint64_t count) {
+        const uint64_t off = (used + 255) & ~255ull;
+        const uint64_t bytes = count * sizeof(T) + 16;
+        if (off > cap || bytes > cap - off) {
+            overflow = true;
+            used = off + bytes;
+            return nullptr;
+        }
+        used = off + bytes;
+        return base ? reinterpret_cast<T*>(base + off) : reinterpret_cast<T*>(16);
+    }
+};
+
+__global__ void single_voxel_kernel(const uint32_t* vox, uint32_t* nodes) {
+    for (int k = 0; k < 8; ++k) nodes[k] = 0;
+    nodes[8] = vox[0];
+    nodes[9] = LEAF;
+}
+
+template <class In>
+int exclusive_scan_static(Arena& a, const In* in, uint64_t n, unsigned* out, cudaStream_t s) {
+    const uint64_t nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
+    if (nb <= 1) {
+        scan_apply_kernel<In><<<1, SCAN_T, 0, s>>>(in, n, nullptr, out);
+        return XN_OK;
+    }
+    unsigned* sums = a.take<unsigned>(nb);
+    unsigned* offs = a.take<unsigned>(nb);
+    if (a.overflow)
+        return fail(XN_ERR_BUDGET, "xn_build_svo_static: the DAG ranks need more than the %llu-byte static scratch",
+                    (unsigned long long)XN_STATIC_SCRATCH_BYTES);
+    scan_reduce_kernel<In><<<(unsigned)nb, SCAN_T, 0, s>>>(in, n, sums);
+    int r = exclusive_scan_static<unsigned>(a, sums, nb, offs, s);
+    if (r) return r;
+    scan_apply_kernel<In><<<(unsigned)nb, SCAN_T, 0, s>>>(in, n, offs, out);
+    return XN_OK;
+}
+
+struct StaticLevels {
+    unsigned long long* size[MAX_LEVELS];
+    unsigned long long* start[MAX_LEVELS];
+    uint32_t* color[MAX_LEVELS];
+    uint8_t* flags[MAX_LEVELS];
+    void* stats_buf[2];
+    unsigned int* counters;
+    unsigned long long* leaf_count;
+    unsigned long long* existing;
+    unsigned long long* ambig_list;
+};
+
+// The scratch every build needs before the node count is known.
+void plan_levels(Arena& a, StaticLevels& p, const LevelGeom* geo, int L, int heuristic) {
+    uint64_t big = 0;
+    for (int d = 0; d < L; ++d) {
+        p.size[d] = a.take<unsigned long long>(geo[d].n);
+        p.start[d] = a.take<unsigned long long>(geo[d].n);
+        p.color[d] = a.take<uint32_t>(geo[d].n);
+        p.flags[d] = a.take<uint8_t>(geo[d].n);
+        big = std::max(big, geo[d].n);
+    }
+    const uint64_t stat_bytes = heuristic == XN_HEUR_STD_DEV ? sizeof(SDStats) : sizeof(CDStats);
+    p.stats_buf[0] = a.take<uint8_t>(big * stat_bytes);
+    p.stats_buf[1] = a.take<uint8_t>(big * stat_bytes);
+    p.counters = a.take<unsigned int>(4);
+    p.leaf_count = a.take<unsigned long long>(1);
+    p.existing = a.take<unsigned long long>(2 * (uint64_t)L);
+    p.ambig_list = heuristic == XN_HEUR_STD_DEV ? a.take<unsigned long long>(big) : nullptr;
+}
+
+int build_static(const uint32_t* d_vox, uint32_t dx, uint32_t dy, uint32_t dz, int type, int heuristic,
+                 double threshold, uint32_t* d_nodes, uint64_t capacity, xn_build_stats* stats, cudaStream_t s) {
+    const uint64_t side = std::max(ceil_pow2(dx), std::max(ceil_pow2(dy), ceil_pow2(dz)));
+    int L = 0;
+    while ((1ull << L) < side) ++L;
+    std::memset(stats, 0, sizeof *stats);
+    stats->side = side;
+    if (L >= MAX_LEVELS) return fail(XN_ERR_ARG, "xn_build_svo_static: grid too large");
+    GridDev g{d_vox, dx, dy, dz};
+    if (L == 0) {
+        stats->total_leaves = stats->unique_leaves = stats->total_nodes = stats->n_nodes = 1;
+        if (capacity < 1) return fail(XN_ERR_ARG, "xn_build_svo_static: the node buffer must hold 1 node");
+        single_voxel_kernel<<<1, 1, 0, s>>>(d_vox, d_nodes);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        return e == cudaSuccess ? XN_OK : cuda_fail(e, "xn_build_svo_static");
+    }
+    LevelGeom geo[MAX_LEVELS];
+    for (int d = 0; d < L; ++d) {
+        const uint64_t e = side >> d;
+        auto box = [&](uint64_t dim) -> uint32_t {
+            if (d == 0) return 1;
+            const uint64_t pe = e * 2;
+            return (uint32_t)std::min<uint64_t>(1ull << d, 2 * ((dim + pe - 1) / pe));
+        };
+        geo[d].bx = box(dx);
+        geo[d].by = box(dy);
+        geo[d].bz = box(dz);
+        geo[d].n = (uint64_t)geo[d].bx * geo[d].by * geo[d].bz;
+        geo[d].e = e;
+    }
+    // size check before anything touches the device
+    StaticLevels p{};
+    Arena measure{nullptr, ~0ull};
+    plan_levels(measure, p, geo, L, heuristic);
+    if (measure.used > XN_STATIC_SCRATCH_BYTES)
+        return fail(XN_ERR_BUDGET,
+                    "xn_build_svo_static: a %ux%ux%u grid needs %llu bytes of build scratch; the static scratch "
+                    "holds %llu (use xn_build_svo)",
+                    dx, dy, dz, (unsigned long long)measure.used, (unsigned long long)XN_STATIC_SCRATCH_BYTES);
+    void* base = nullptr;
+    int r = static_scratch_address(&base);
+    if (r) return r;
+    Arena a{static_cast<unsigned char*>(base), XN_STATIC_SCRATCH_BYTES};
+    plan_levels(a, p, geo, L, heuristic);
+
+    cudaError_t e = cudaSuccess;
+    const unsigned T = 256;
+    for (int d = L - 1; d >= 0 && e == cudaSuccess; --d) {
+        UpArgs u{};
+        u.g = g;
+        u.cur = geo[d];
+        u.child_is_voxel = d == L - 1;
+        if (d < L - 1) u.child = geo[d + 1];
+        u.child_stats = p.stats_buf[(d + 1) & 1];
+        u.stats = p.stats_buf[d & 1];
+        u.child_size = d < L - 1 ? p.size[d + 1] : nullptr;
+        u.size = p.size[d];
+        u.color = p.color[d];
+        u.flags = p.flags[d];
+        u.chan_diff = (uint32_t)(uint8_t)threshold;
+        u.stddev = threshold;
+        u.ambig_count = p.counters;
+        u.ambig_list = p.ambig_list;
+        if (heuristic == XN_HEUR_STD_DEV) {
+            unsigned int amb = 0;
+            e = cudaMemsetAsync(p.counters, 0, 4, s);
+            if (e != cudaSuccess) break;
+            up_level_kernel<XN_HEUR_STD_DEV><<<blocks_for(geo[d].n, T), T, 0, s>>>(u);
+            if ((e = cudaMemcpyAsync(&amb, p.counters, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+            if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
+            if (amb) {
+                stddev_fixup_kernel<<<blocks_for(amb, 64), 64, 0, s>>>(u, amb);
+                resize_level_kernel<<<blocks_for(geo[d].n, T), T, 0, s>>>(u);
+            }
+        } else {
+            up_level_kernel<XN_HEUR_CHANNEL_DIFF><<<blocks_for(geo[d].n, T), T, 0, s>>>(u);
+        }
+        e = cudaGetLastError();
+    }
+    unsigned long long n_total = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&n_total, p.size[0], 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "xn_build_svo_static: bottom-up pass");
+    if (n_total > 0xFFFFFFFFull) return fail(XN_ERR_FORMAT, "xn_build_svo_static: more than 2^32 nodes");
+    const bool dag = type == XN_SVO_DAG;
+    stats->n_nodes = n_total;
+    if (!dag && n_total > capacity)
+        return fail(XN_ERR_ARG, "xn_build_svo_static: the octree has %llu nodes; the node buffer holds %llu",
+                    (unsigned long long)n_total, (unsigned long long)capacity);
+
+    for (int d = 0; d < L && e == cudaSuccess; ++d) e = cudaMemsetAsync(p.start[d], 0xFF, geo[d].n * 8, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p.start[0], 0, 8, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p.counters, 0, 16, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p.leaf_count, 0, 8, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p.existing, 0, 16 * (uint64_t)L, s);
+    for (int d = 0; d < L && e == cudaSuccess; ++d) {
+        DownArgs w{};
+        w.g = g;
+        w.cur = geo[d];
+        w.child_is_voxel = d == L - 1;
+        if (d < L - 1) w.child = geo[d + 1];
+        w.depth = d;
+        w.n_total = n_total;
+        w.size = p.size[d];
+        w.child_size = d < L - 1 ? p.size[d + 1] : nullptr;
+        w.color = p.color[d];
+        w.flags = p.flags[d];
+        w.start = p.start[d];
+        w.child_start = d < L - 1 ? p.start[d + 1] : nullptr;
+        w.nodes = dag ? nullptr : d_nodes;
+        w.leaves = p.leaf_count;
+        w.max_depth = p.counters + 1;
+        w.existing = p.existing + 2 * d;
+        down_level_kernel<<<blocks_for(geo[d].n, T), T, 0, s>>>(w);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && type == XN_SVO_ROPE_TREE) {
+        RopeArgs ra{};
+        ra.L = L;
+        ra.n_total = n_total;
+        ra.nodes = d_nodes;
+        for (int d = 0; d < L; ++d) ra.lv[d] = LevelDev{geo[d], p.size[d], p.start[d], p.flags[d]};
+        for (int d = 0; d < L && e == cudaSuccess; ++d) {
+            rope_level_kernel<<<blocks_for(geo[d].n, 128), 128, 0, s>>>(ra, d);
+            e = cudaGetLastError();
+        }
+    }
+    unsigned long long leaves = 0;
+    unsigned int hc[2] = {0, 0};
+    unsigned long long hexist[2 * MAX_LEVELS];
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&leaves, p.leaf_count, 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hc, p.counters, 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hexist, p.existing, 16 * (uint64_t)L, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "xn_build_svo_static: top-down pass");
+    stats->total_leaves = leaves;
+    stats->unique_leaves = leaves;
+    stats->total_nodes = n_total;
+    stats->depth = hc[1];
+    if (!dag) return XN_OK;
+
+    // DAG classes, ranks and nodes, with the same kernels as xn_build_svo
+    unsigned long long* canon[MAX_LEVELS + 1];
+    uint64_t tsize_max = 1;
+    for (int d = 0; d <= L; ++d) {
+        const uint64_t ids = d < L ? geo[d].n : 8 * geo[L - 1].n;
+        canon[d] = a.take<unsigned long long>(ids);
+        const uint64_t count = d < L ? hexist[2 * d] : 8 * hexist[2 * (L - 1) + 1];
+        uint64_t ts = 1;
+        while (ts < 2 * count) ts <<= 1;
+        tsize_max = std::max(tsize_max, ts);
+    }
+    Slot* table = a.take<Slot>(tsize_max);
+    uint8_t* is_rep = a.take<uint8_t>(n_total);
+    unsigned* ins = a.take<unsigned>(n_total);
+    if (a.overflow)
+        return fail(XN_ERR_BUDGET,
+                    "xn_build_svo_static: the DAG of this %ux%ux%u grid needs more than the %llu-byte static scratch "
+                    "(use xn_build_svo)",
+                    dx, dy, dz, (unsigned long long)XN_STATIC_SCRATCH_BYTES);
+    auto level_of = [&](int d) {
+        DagLevel q{};
+        q.depth = d;
+        q.L = L;
+        q.g = g;
+        const int cd = d < L ? d : L - 1;
+        q.geom = geo[cd];
+        q.start = p.start[cd];
+        q.size = p.size[cd];
+        q.color = p.color[cd];
+        q.flags = p.flags[cd];
+        q.canon = canon[d];
+        if (d < L) {
+            q.child_is_voxel = d == L - 1;
+            q.child_canon = canon[d + 1];
+            if (d < L - 1) q.child_geom = geo[d + 1];
+        }
+        return q;
+    };
+    for (int d = L; d >= 0 && e == cudaSuccess; --d) {
+        const uint64_t count = d < L ? hexist[2 * d] : 8 * hexist[2 * (L - 1) + 1];
+        if (count == 0) continue;
+        uint64_t ts = 1;
+        while (ts < 2 * count) ts <<= 1;
+        const uint64_t ids = d < L ? geo[d].n : 8 * geo[L - 1].n;
+        e = cudaMemsetAsync(table, 0xFF, ts * sizeof(Slot), s);
+        if (e != cudaSuccess) break;
+        dag_insert_kernel<<<blocks_for(ids, T), T, 0, s>>>(level_of(d), table, ts - 1, p.counters);
+        dag_lookup_kernel<<<blocks_for(ids, T), T, 0, s>>>(level_of(d), table, ts - 1, p.counters);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemsetAsync(is_rep, 0, n_total, s);
+    for (int d = L; d >= 0 && e == cudaSuccess; --d) {
+        const uint64_t ids = d < L ? geo[d].n : 8 * geo[L - 1].n;
+        dag_mark_kernel<<<blocks_for(ids, T), T, 0, s>>>(level_of(d), is_rep);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "xn_build_svo_static: DAG classes");
+    if ((r = exclusive_scan_static<uint8_t>(a, is_rep, n_total, ins, s))) return r;
+    unsigned last_ins = 0;
+    uint8_t last_rep = 0;
+    unsigned int ovf = 0;
+    e = cudaMemcpyAsync(&last_ins, ins + (n_total - 1), 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&last_rep, is_rep + (n_total - 1), 1, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&ovf, p.counters, 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "xn_build_svo_static: DAG ranks");
+    if (ovf) return fail(XN_ERR_STATE, "xn_build_svo_static: DAG hash table overflow (0x%x)", ovf);
+    const uint64_t U = (uint64_t)last_ins + last_rep;
+    stats->n_nodes = U;
+    if (U > capacity)
+        return fail(XN_ERR_ARG, "xn_build_svo_static: the DAG has %llu nodes; the node buffer holds %llu",
+                    (unsigned long long)U, (unsigned long long)capacity);
+    e = cudaMemsetAsync(p.leaf_count, 0, 8, s);
+    for (int d = L; d >= 0 && e == cudaSuccess; --d) {
+        const uint64_t ids = d < L ? geo[d].n : 8 * geo[L - 1].n;
+        dag_write_kernel<<<blocks_for(ids, T), T, 0, s>>>(level_of(d), ins, U, d_nodes, p.leaf_count);
+        e = cudaGetLastError();
+    }
+    unsigned long long ul = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&ul, p.leaf_count, 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "xn_build_svo_static: DAG write");
+    stats->unique_leaves = ul;
+    return XN_OK;
+}
+
+}  // namespace
+}  // namespace xn
+
+XN_API int xn_build_svo_static(const uint32_t* d_rgba, uint32_t dx, uint32_t dy, uint32_t dz, int type,
+                               int heuristic, double threshold, uint32_t* d_nodes, uint64_t node_capacity,
+                               xn_build_stats* stats, void* stream) {
+    if (!d_rgba || !d_nodes || !stats) return fail(XN_ERR_ARG, "xn_build_svo_static: NULL argument");
+    if (!dx || !dy || !dz) return fail(XN_ERR_ARG, "xn_build_svo_static: empty grid %ux%ux%u", dx, dy, dz);
+    if (type < XN_SVO_SPARSE || type > XN_SVO_ROPE_TREE)
+        return fail(XN_ERR_ARG, "xn_build_svo_static: invalid type %d", type);
+    if (heuristic == XN_HEUR_CHANNEL_DIFF) {
+        if (!(threshold >= 0.0 && threshold <= 255.0) || threshold != (double)(int)threshold)
+            return fail(XN_ERR_ARG, "xn_build_svo_static: --chan-diff must be an integer in 0..255");
+    } else if (heuristic == XN_HEUR_STD_DEV) {
+        if (!(threshold >= 0.0)) return fail(XN_ERR_ARG, "xn_build_svo_static: --std-dev must be >= 0");
+    } else {
+        return fail(XN_ERR_ARG, "xn_build_svo_static: invalid heuristic %d", heuristic);
+    }
+    if ((reinterpret_cast<uintptr_t>(d_rgba) & 3) || (reinterpret_cast<uintptr_t>(d_nodes) & 7))
+        return fail(XN_ERR_ARG, "xn_build_svo_static: the grid must be 4-byte and the node buffer 8-byte aligned");
+    return xn::build_static(d_rgba, dx, dy, dz, type, heuristic, threshold, d_nodes, node_capacity, stats,
+                            static_cast<cudaStream_t>(stream));
+}
