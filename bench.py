@@ -206,6 +206,194 @@ def run_reference(args):
     return 0
 
 
+def measure_batched(ctx, xg, args):
+    """Many cameras in one persistent launch vs one launch per frame.
+
+    The 1024^3 gas-field workload: a log-normal density field (P(k) ~ k^-2.5,
+    seed 2) built into a rope octree on the device, rendered with esvo and
+    svo-rope from 64 cameras on a Fibonacci sphere at 1.8x the extent, 45 deg
+    vertical field of view, 1920x1080."""
+    import torch
+    from xenodon_gb300 import cameras, volumes
+    n = args.batched_size
+    t0 = time.time()
+    g = volumes.gas_field(n, seed=2, device="cuda", as_tensor=True)
+    vol, st = ctx.build_svo_volume(g.data_ptr(), (n, n, n), "rope")
+    build_s = time.time() - t0
+    dda4k = measure_dda_4k(ctx, xg, g, n)
+    del g
+    torch.cuda.empty_cache()
+    w, h = 1920, 1080
+    cams = cameras.fibonacci_sphere(args.batched_cameras, np.array([0.5, 0.5, 0.5]), 1.8,
+                                    cameras.forward_length_for_vfov(45.0, w, h))
+    params = xg.make_params(w, h, EMISSION)
+    trav = ("esvo", "svo-rope")
+    specs = [(vol, t, xg.make_camera(*c), params) for t in trav for c in cams]
+    bufs = [torch.empty((h, w), dtype=torch.int32, device="cuda") for _ in specs]
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    rays = w * h * len(specs)
+
+    def plain():
+        for (v, t, c, p), b in zip(specs, bufs):
+            ctx.render_device(v, t, c, p, b.data_ptr(), None, None, sptr)
+
+    def timed(fn, reps=2):
+        fn()
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        return best
+
+    plain_ms = timed(plain)
+    plain_out = [b.clone() for b in bufs[:: max(1, len(bufs) // 8)]]
+    jobs = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs, bufs))
+    # tune the launch shape on a slice of the batch
+    k = min(16, len(specs))
+    tune_jobs = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs[::len(specs) // k], bufs))
+    best, _ = ctx.autotune_batch(tune_jobs, k, sptr)
+    graph = ctx.batch_graph(len(specs), best, sptr)
+    for b in bufs:
+        b.fill_(-1)
+    batched_ms = timed(lambda: graph.launch(jobs, len(specs)))
+    same = all(torch.equal(a, b) for a, b in zip(plain_out, bufs[:: max(1, len(bufs) // 8)]))
+    graph.close()
+    vol.release()
+    return {
+        "workload": f"{n}^3 gas field, rope octree, esvo+svo-rope, {len(cams)} Fibonacci-sphere cameras at 1.8x, "
+                    f"45 deg VFOV, {w}x{h}",
+        "octree_nodes": st["n_nodes"], "volume_build_s": round(build_s, 2), "frames": len(specs),
+        "plain_ms": round(plain_ms, 3), "batched_ms": round(batched_ms, 3),
+        "plain_mrays_s": round(rays / (plain_ms * 1e3), 1), "batched_mrays_s": round(rays / (batched_ms * 1e3), 1),
+        "speedup": round(plain_ms / batched_ms, 3), "identical_images": bool(same), "launch_shape": best.as_dict(),
+        "dda_4k": dda4k,
+    }
+
+
+def measure_dda_4k(ctx, xg, g, n):
+    """Plain DDA on the n^3 gas-field grid at 3840x2160 from 8 orbit cameras at
+    2x the extent: Mrays/s and the fraction of the HBM roofline (4 B per texel
+    the reference reads + 4 B per pixel, over the measured HBM copy bandwidth)."""
+    import torch
+    from xenodon_gb300 import cameras
+    vol = ctx.upload_grid_device(g.data_ptr(), (n, n, n))
+    w, h = 3840, 2160
+    params = xg.make_params(w, h, EMISSION)
+    cams = [xg.make_camera(*c) for c in cameras.orbit(np.array([0.5, 0.5, 0.5]), 2.0, 8)]
+    out = torch.empty((h, w), dtype=torch.int32, device="cuda")
+    loads = torch.empty((h, w), dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    for c in cams[:3]:
+        ctx.render_device(vol, "dda", c, params, out.data_ptr(), None, None, sptr)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in cams]
+    for c, (a, b) in zip(cams, evs):
+        a.record(stream)
+        ctx.render_device(vol, "dda", c, params, out.data_ptr(), None, None, sptr)
+        b.record(stream)
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in evs]
+    words = 0
+    for c in cams:
+        ctx.render_device(vol, "dda", c, params, out.data_ptr(), None, loads.data_ptr(), sptr)
+        words += int(loads.to(torch.int64).sum().item())
+    torch.cuda.synchronize()
+    vol.release()
+    total_ms = sum(ms)
+    alg = 4.0 * words + 4.0 * w * h * len(cams)
+    gbs = alg / (total_ms * 1e-3) / 1e9
+    peak = load_peaks()["hbm_gbs"]
+    return {"workload": f"dda, {n}^3 gas-field grid, {w}x{h}, 8 orbit cameras at 2x the extent",
+            "ms_per_frame": round(total_ms / len(cams), 4), "mrays_s": round(w * h * len(cams) / (total_ms * 1e3), 1),
+            "algorithmic_gbs": round(gbs, 1), "hbm_frac": round(gbs / peak, 4),
+            "texels_per_ray": round(words / (w * h * len(cams)), 1)}
+
+
+def measure_serving(ctx, xg, args, scene):
+    """Continuous batching of a request mix vs one frame per launch.
+
+    Requests draw a volume (the CT grid and octree, the 128^3 blob grid and its
+    octree), a traversal valid for it, a resolution from {256^2, 512^2,
+    1280x720, 1920x1080, 3840x2160} and a camera on a sphere at 1.2-3x the
+    extent; arrivals are Poisson at each swept rate (seed 4)."""
+    import torch
+    from xenodon_gb300 import cameras, volumes
+    rng = np.random.default_rng(4)
+    blobs = volumes.blobs(128, seed=0)
+    bnodes, bst = ctx.build_svo(blobs, "rope", "chan-diff", 0)
+    ct_grid, ct_nodes, ct_side = scene
+    vols = {1: ("grid", ct_grid), 2: ("svo", (ct_nodes, ct_side)), 3: ("grid", blobs), 4: ("svo", (bnodes, bst["side"]))}
+    res = [(256, 256), (512, 512), (1280, 720), (1920, 1080), (3840, 2160)]
+    svo_t = ("svo-naive", "esvo", "svo-df", "svo-rope")
+
+    def draw():
+        vid = int(rng.integers(1, 5))
+        trav = "dda" if vols[vid][0] == "grid" else svo_t[int(rng.integers(0, 4))]
+        w, h = res[int(rng.integers(0, len(res)))]
+        dims = vols[vid][1].shape[2::-1] if vols[vid][0] == "grid" else None
+        centre = cameras.volume_centre(dims) if dims is not None else np.array([0.5, 0.5, 0.5])
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        cam = cameras.look_at(centre + d * rng.uniform(1.2, 3.0), centre)
+        return vid, trav, cam, xg.make_params(w, h, EMISSION)
+
+    n_req = args.serve_requests
+    reqs = [draw() for _ in range(n_req)]
+    # plain: one frame per launch, back to back
+    handles = {}
+    for vid, (kind, d) in vols.items():
+        handles[vid] = ctx.upload_grid(d) if kind == "grid" else ctx.upload_svo(d[0], d[1])
+    outs = [np.empty((p.output_region.height, p.output_region.width, 4), np.uint8) for _, _, _, p in reqs]
+    for vid, t, c, p in reqs[:5]:
+        ctx.render(handles[vid], t, xg.make_camera(*c), p)
+    t0 = time.perf_counter()
+    for (vid, t, c, p), o in zip(reqs, outs):
+        ctx.render(handles[vid], t, xg.make_camera(*c), p, out=o)
+    plain_s = time.perf_counter() - t0
+    rays = sum(p.output_region.width * p.output_region.height for _, _, _, p in reqs)
+    for h in handles.values():
+        h.release()
+    result = {"workload": "request mix over the CT grid/octree and the 128^3 blob grid/octree; resolutions "
+                          "256^2..3840x2160; cameras at 1.2-3x the extent",
+              "requests": n_req, "plain_mrays_s": round(rays / plain_s / 1e6, 1), "rates": []}
+    for rate in args.serve_rates:
+        with xg.Server(ctx, hbm_budget=150 << 30, max_batch_jobs=64, streams=2) as srv:
+            for vid, (kind, d) in vols.items():
+                if kind == "grid":
+                    srv.add_grid(vid, d)
+                else:
+                    srv.add_svo(vid, d[0], d[1])
+            gaps = rng.exponential(1.0 / rate, n_req) if rate > 0 else np.zeros(n_req)
+            tickets = []
+            start = time.perf_counter()
+            next_t = start
+            for (vid, t, c, p), gap in zip(reqs, gaps):
+                next_t += gap
+                while time.perf_counter() < next_t:
+                    pass
+                tickets.append(srv.submit(vid, t, xg.make_camera(*c), p))
+            same = True
+            for i, tk in enumerate(tickets):
+                img, _ = srv.wait(tk, timeout=120)
+                if i % 17 == 0:
+                    same &= bool(np.array_equal(img, outs[i]))
+            st = srv.stats()
+        result["rates"].append({"offered_req_s": rate if rate > 0 else "closed", "p50_ms": round(st["p50_ms"], 3),
+                                "p99_ms": round(st["p99_ms"], 3), "mrays_s": round(st["mrays_per_s"], 1),
+                                "mean_batch": round(st["mean_batch"], 2), "identical_images": same})
+    sat = max(r["mrays_s"] for r in result["rates"])
+    result["served_vs_plain"] = round(sat / result["plain_mrays_s"], 3)
+    return result
+
+
 def run_ours(args):
     import torch
     import xenodon_gb300 as xg
@@ -330,6 +518,13 @@ def run_ours(args):
         "clocks": clk.summary(),
         "build": {"svo_build_s": round(build_s, 3), "volume_gen_s": round(gen_s, 2)},
     }
+    if rank == 0 and not args.no_extras:
+        for key, fn in (("batched", lambda: measure_batched(ctx, xg, args)),
+                        ("serving", lambda: measure_serving(ctx, xg, args, (grid, nodes, st["side"])))):
+            try:
+                line[key] = fn()
+            except Exception as exc:  # the headline line is printed regardless
+                line[key] = {"error": f"{type(exc).__name__}: {exc}"}
     if rank == 0 and not args.no_cpu_baseline:
         import oracle
         oracle.build()
@@ -356,9 +551,12 @@ def main(argv=None):
     ap.add_argument("--cpu-row-step", type=int, default=20)
     ap.add_argument("--ref-row-step", type=int, default=60)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched and serving measurements")
+    ap.add_argument("--batched-size", type=int, default=1024)
+    ap.add_argument("--batched-cameras", type=int, default=64)
+    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 200.0, 1000.0, 0.0])
     args = ap.parse_args(argv)
-    if args.warmup < 3:
-        ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -128,6 +128,9 @@ XN_API int xn_volume_upload_grid(xn_ctx* ctx, const uint8_t* rgba, uint32_t dx, 
  * device for traversal. */
 XN_API int xn_volume_upload_svo(xn_ctx* ctx, const uint32_t* nodes, uint64_t n_nodes, uint64_t side,
                                 xn_volume** out);
+/* xn_volume_upload_grid from a grid already in device memory (no host copy). */
+XN_API int xn_volume_upload_grid_device(xn_ctx* ctx, const void* d_rgba, uint32_t dx, uint32_t dy, uint32_t dz,
+                                        xn_volume** out);
 XN_API int xn_volume_release(xn_volume* vol);
 XN_API int xn_volume_info_get(const xn_volume* vol, xn_volume_info* info);
 
@@ -157,6 +160,83 @@ XN_API int xn_render_device(xn_ctx* ctx, const xn_volume* vol, int traversal, co
                             const xn_params* params, void* d_rgba, float* d_emission,
                             uint32_t* d_loads, void* stream);
 
+/* ---------------------------------------------------------- batching --- */
+
+/* One frame of a batch (no counterpart in the reference, which renders one
+ * frame per dispatch): a volume, a traversal, a camera, the regions, and a
+ * caller-owned device buffer of output_region.width*height*4 bytes. */
+typedef struct {
+    const xn_volume* volume;
+    int traversal;
+    xn_camera camera;
+    xn_params params;
+    void* d_rgba;
+} xn_job;
+
+/* Launch shape of the persistent batch kernel. */
+typedef struct {
+    uint32_t tile_width;    /* warp tile width in pixels: 4, 8, 16 or 32 (height = 32/width) */
+    uint32_t block_threads; /* threads per block: a multiple of 32, at most 1024 */
+    uint32_t blocks_per_sm; /* resident blocks per SM; 0 = as many as fit */
+    uint32_t chunk;         /* warp tiles a warp takes per pop of the work queue, >= 1 */
+} xn_batch_config;
+
+/* Renders n_jobs frames of any mix of volumes, traversals and resolutions in
+ * one persistent launch on `stream` (returns without synchronising): resident
+ * warps pull tiles from one global queue.  cfg NULL = the configuration the
+ * autotuner chose for this mix of traversals, else a default. */
+XN_API int xn_render_batch(xn_ctx* ctx, const xn_job* jobs, int n_jobs, const xn_batch_config* cfg, void* stream);
+
+/* Times xn_render_batch over a sweep of launch shapes on the given jobs and
+ * keeps the fastest for their mix of traversals (used when cfg is NULL). */
+XN_API int xn_autotune_batch(xn_ctx* ctx, const xn_job* jobs, int n_jobs, void* stream, xn_batch_config* best,
+                             float* best_ms);
+
+/* A batch launch captured once as a CUDA graph (job-table upload, queue reset,
+ * persistent kernel) and replayed per batch; two graph instances alternate so
+ * the host fills the next job table while the previous batch runs. */
+typedef struct xn_batch_graph xn_batch_graph;
+XN_API int xn_batch_graph_create(xn_ctx* ctx, int capacity_jobs, const xn_batch_config* cfg, void* stream,
+                                 xn_batch_graph** out);
+XN_API int xn_batch_graph_launch(xn_batch_graph* g, const xn_job* jobs, int n_jobs);
+XN_API int xn_batch_graph_destroy(xn_batch_graph* g);
+
+/* ----------------------------------------------------------- serving --- */
+
+/* A render server (no counterpart in the reference): a worker thread keeps
+ * registered volumes resident with least-recently-used eviction under an HBM
+ * budget, admits requests in arrival order as memory allows, renders each
+ * admitted set as one persistent batch on one of `streams` CUDA streams, and
+ * admits newly arrived requests while earlier batches are still running. */
+typedef struct xn_server xn_server;
+typedef struct {
+    uint64_t hbm_budget; /* bytes for resident volumes and in-flight frames; 0 = the context's budget */
+    int max_batch_jobs;  /* requests per persistent launch (default 256) */
+    int streams;         /* batches in flight at once (default 2) */
+} xn_server_config;
+typedef struct {
+    uint64_t completed, failed, batches, uploads, evictions, rays, hbm_used;
+    double mean_batch;   /* requests per batch */
+    double p50_ms, p99_ms, max_ms; /* submit -> result in host memory */
+    double mrays_per_s;  /* rays of completed requests / time from the first submit to the last result */
+} xn_server_metrics;
+
+XN_API int xn_server_create(xn_ctx* ctx, const xn_server_config* cfg, xn_server** out);
+XN_API int xn_server_destroy(xn_server* server);
+/* Register a volume by id; the host copy is kept so the volume can be
+ * uploaded again after an eviction. */
+XN_API int xn_server_add_grid(xn_server* server, uint32_t volume_id, const uint8_t* rgba, uint32_t dx, uint32_t dy,
+                              uint32_t dz);
+XN_API int xn_server_add_svo(xn_server* server, uint32_t volume_id, const uint32_t* nodes, uint64_t n_nodes,
+                             uint64_t side);
+/* Queue a frame; out_rgba (width*height*4 bytes of host memory) must stay
+ * valid until xn_server_wait returns for the ticket. */
+XN_API int xn_server_submit(xn_server* server, uint32_t volume_id, int traversal, const xn_camera* cam,
+                            const xn_params* params, uint8_t* out_rgba, uint64_t* ticket);
+/* Wait for a ticket (timeout_s < 0: no limit); releases the ticket. */
+XN_API int xn_server_wait(xn_server* server, uint64_t ticket, double timeout_s, double* latency_ms);
+XN_API int xn_server_stats(xn_server* server, xn_server_metrics* out);
+
 /* Error bits raised by rays since the last call (1 = iteration cap, 2 = stack
  * limit); reset clears them.  Synchronises the context's device. */
 XN_API int xn_ray_errors(xn_ctx* ctx, uint32_t* bits, int reset);
@@ -172,6 +252,13 @@ XN_API int xn_build_svo(xn_ctx* ctx, const uint8_t* rgba, uint32_t dx, uint32_t 
                         int type, int heuristic, double threshold, uint32_t** nodes_out,
                         xn_build_stats* stats);
 XN_API void xn_free(void* p);
+
+/* `xenodon convert` followed by an upload, without leaving the device: builds
+ * the octree of a grid in device memory (d_rgba: packed RGBA8 texels, x
+ * fastest) and makes it a resident volume.  The node array is the one
+ * xn_build_svo returns. */
+XN_API int xn_build_svo_volume(xn_ctx* ctx, const void* d_rgba, uint32_t dx, uint32_t dy, uint32_t dz, int type,
+                               int heuristic, double threshold, xn_volume** out, xn_build_stats* stats);
 
 /* No counterpart in the reference.  The same octree build as xn_build_svo, for
  * callers that cannot allocate device memory: code that runs inside another

@@ -101,3 +101,28 @@ def test_gpu_built_octree_renders_like_oracle_built(ctx):
     o = oracle.render("svo-rope", nodes=ref, camera=oracle.make_camera((0, 0, -0.8660254), (0, 1, 0), (0.5, 0.5, 2.5)),
                       view=oracle.make_view(64, 64, 10.0))
     assert np.abs(rgba.astype(int) - o["rgba"].astype(int)).max() <= 1
+
+
+def test_device_resident_build_and_upload_match_host_paths(ctx):
+    import torch
+    import xenodon_gb300 as xg
+    from xenodon_gb300 import volumes
+    g = volumes.blobs(48, seed=8)
+    d = torch.from_numpy(g).cuda().contiguous()
+    dims = (g.shape[2], g.shape[1], g.shape[0])
+    svo_dev, st = ctx.build_svo_volume(d.data_ptr(), dims, "rope")
+    nodes, st_host = ctx.build_svo(g, "rope")
+    assert st == st_host
+    svo_host = ctx.upload_svo(nodes, st_host["side"])
+    grid_dev = ctx.upload_grid_device(d.data_ptr(), dims)
+    grid_host = ctx.upload_grid(g)
+    assert svo_dev.info()["device_bytes"] == svo_host.info()["device_bytes"]
+    cam = xg.make_camera((0.3, -0.1, -0.95), (0, 1, -0.105), (0.2, 0.7, 2.2))
+    p = xg.make_params(80, 60, 10.0)
+    for t in ("svo-naive", "esvo", "svo-df", "svo-rope"):
+        a, _, _ = ctx.render(svo_dev, t, cam, p)
+        b, _, _ = ctx.render(svo_host, t, cam, p)
+        assert np.array_equal(a, b), t
+    a, _, _ = ctx.render(grid_dev, "dda", cam, p)
+    b, _, _ = ctx.render(grid_host, "dda", cam, p)
+    assert np.array_equal(a, b)

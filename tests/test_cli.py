@@ -1,0 +1,109 @@
+"""The `xenodon` command line: argv, configuration and error behaviour of the
+reference's `render` and `convert` (src/main.cpp:97-196, src/convert.cpp:13-122,
+src/core/Config.h).  CPU only: every case fails before the GPU is touched."""
+from __future__ import annotations
+
+import subprocess
+
+import pytest
+
+from xenodon_gb300 import CLI_PATH
+
+
+def run(*args, cwd=None):
+    p = subprocess.run([str(CLI_PATH), *args], capture_output=True, text=True, cwd=cwd, timeout=60)
+    return p.returncode, p.stdout
+
+
+@pytest.fixture(scope="module")
+def conf(tmp_path_factory, built_library):
+    d = tmp_path_factory.mktemp("cli")
+    (d / "ok.conf").write_text("device {\n    vkindex = 0\n    offset = (0, 0)\n    extent = (64, 48)\n}\n")
+    return d
+
+
+@pytest.mark.parametrize("args,msg", [
+    ((), "Missing required positional argument <volume path>"),
+    (("v.svo",), "Missing required backend --xorg, --headless or --direct"),
+    (("--headless", "ok.conf", "--xorg", "v.svo"), "--xorg, --headless and --direct are mutually exclusive"),
+    (("--discard-output", "v.svo", "--xorg"), "--dont-save requires --headless"),
+    (("--output", "x.png", "--xorg", "v.svo"), "--output requires --headless"),
+    (("--headless", "ok.conf", "--discard-output", "--output", "a.png", "v.svo"),
+     "--dont-save and --output are mutually exclusive"),
+    (("--headless", "ok.conf", "-e", "-1", "v.svo"), "Invalid value for <emission coefficient> of parameter -e"),
+    (("--headless", "ok.conf", "-e", "1e3", "v.svo"), "Invalid value for <emission coefficient> of parameter -e"),
+    (("--headless", "ok.conf", "-e", "1", "--emission-coeff", "2", "v.svo"),
+     "Duplicate specification of parameter --emission-coeff/-e"),
+    (("--headless", "ok.conf", "-q", "-q", "v.svo"), "Duplicate specification of flag --quiet/-q"),
+    (("--headless", "ok.conf", "-r", "1:2", "v.svo"), "Invalid value for <voxel dimension ratio> of parameter -r"),
+    (("--headless", "ok.conf", "-r", "1:0:2", "v.svo"), "Invalid value for <voxel dimension ratio> of parameter -r"),
+    (("--headless", "ok.conf", "--repeat", "0", "v.svo"), "Invalid value for <frame repeat> of parameter --repeat"),
+    (("--headless", "ok.conf", "--backend", "vulkan", "v.svo"), "Invalid value for <backend> of parameter --backend"),
+    (("--headless", "ok.conf", "v.svo", "w.svo"), "Unexpected positional argument 'w.svo'"),
+    (("--headless", "ok.conf", "--bogus", "v.svo"), "Unrecognized option --bogus"),
+    (("--headless", "ok.conf", "--camera"), "Parameter --camera expects argument <camera>"),
+    (("--headless", "ok.conf", "-q", "v.xyz"), "Failed to parse model file type"),
+    (("--headless", "ok.conf", "-q", "-s", "svo-naive", "v.tif"),
+     "Shader 'svo-naive' is incompatible with model type 'tiff' (requires 'svo')"),
+    (("--headless", "ok.conf", "-q", "-s", "dda", "v.svo"),
+     "Shader 'dda' is incompatible with model type 'svo' (requires 'tiff')"),
+    (("--headless", "ok.conf", "-q", "-s", "nope", "v.svo"), "Invalid shader 'nope'"),
+    (("--headless", "ok.conf", "-q", "--volume-type", "raw", "v.svo"), "Failed to parse model file type"),
+])
+def test_render_argument_errors(conf, args, msg):
+    rc, out = run("render", *args, cwd=conf)
+    assert rc == 1
+    assert f"Error: {msg}" in out
+
+
+@pytest.mark.parametrize("text,msg", [
+    ("", "Configuration error: At least one device entry is required"),
+    ("device {\n vkindex = 0\n offset = (0, 0)\n}\n", "Configuration error: Missing key 'extent'"),
+    ("device {\n vkindex = 0\n vkindex = 1\n offset = (0, 0)\n extent = (1, 1)\n}\n",
+     "Configuration error: Ambiguous key 'vkindex'"),
+    ("device {\n vkindex = 0 # note\n}\n", "Parse error at line 2, col 14: Unexpected character '#'"),
+    ("monitor {\n}\n", "Unexpected key 'monitor'"),
+    ("device {\n vkindex = x\n}\n", "Expected numeric character, found 'x'"),
+    ("device {\n vkindex = 0\n offset = (0 0)\n extent = (1, 1)\n}\n", "Expected character ',', found '0'"),
+    ("device {\n vkindex = 0\n offset = (0, 0)\n extent = (1, 1)\n}\n}", "Expected end of input, found '}'"),
+])
+def test_headless_config_errors(conf, text, msg):
+    (conf / "bad.conf").write_text(text)
+    rc, out = run("render", "--headless", "bad.conf", "v.svo", cwd=conf)
+    assert rc == 1
+    assert "Error: Failed to initialize backend: Failed to read config file 'bad.conf': " in out
+    assert msg in out
+
+
+def test_missing_config_file(conf):
+    rc, out = run("render", "--headless", "nope.conf", "v.svo", cwd=conf)
+    assert "Error: Failed to initialize backend: Failed to open config file 'nope.conf'" in out
+
+
+@pytest.mark.parametrize("args,msg", [
+    (("--dag", "--rope", "a.tif", "b.svo"), "--dag and --rope are mutually exclusive"),
+    (("--chan-diff", "3", "--std-dev", "2", "a.tif", "b.svo"), "--std-dev and --chan-diff are mutually exclusive"),
+    (("--chan-diff", "256", "a.tif", "b.svo"), "Invalid value for <channel difference> of parameter --chan-diff"),
+    (("--std-dev", "-1", "a.tif", "b.svo"), "Invalid value for <std. dev> of parameter --std-dev"),
+    (("a.tif",), "Missing required positional argument <destination svo path>"),
+])
+def test_convert_argument_errors(conf, args, msg):
+    rc, out = run("convert", *args, cwd=conf)
+    assert rc == 1 and f"Error: {msg}" in out
+
+
+def test_convert_missing_source(conf):
+    rc, out = run("convert", "nope.tif", "out.svo", cwd=conf)
+    assert out.startswith("Loading source...\n")
+    assert "Error reading 'nope.tif': Failed to open" in out
+
+
+def test_help_and_unknown_subcommand(built_library):
+    rc, out = run()
+    assert rc == 0 and "render" in out and "convert" in out
+    rc, out = run("help", "render")
+    assert rc == 0 and "--headless" in out
+    rc, out = run("help", "nope")
+    assert rc == 1 and "Error: No such topic nope" in out
+    rc, out = run("bogus")
+    assert rc == 1 and "Error: Invalid subcommand 'bogus'" in out

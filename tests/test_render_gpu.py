@@ -188,3 +188,92 @@ def test_hbm_budget_refuses_uploads(built_library, blob_volumes):
             c.upload_grid(g)
         assert e.value.code == xg.XN_ERR_BUDGET
         assert c.memory()[0] < g.nbytes // 2
+
+
+@pytest.mark.parametrize("cam", ["front", "inside", "grazing"])
+def test_parity_dda_linear_grid_layout(ctx, blob_volumes, monkeypatch, cam):
+    # the linear (x-fastest global memory) form of the grid, beside the default texture form
+    import xenodon_gb300 as xg
+    g, _, _ = blob_volumes
+    monkeypatch.setenv("XN_GRID_LAYOUT", "linear")
+    vol = ctx.upload_grid(g)
+    assert vol.info()["device_bytes"] == g.nbytes
+    p, v = _params_pair(xg, 96, 64)
+    check_parity(ctx, "dda", CAMS[cam], p, v, grid=g, vol=vol, label=f"linear/{cam}")
+
+
+def test_octree_device_layout_is_compact(ctx, blob_volumes):
+    # the reference's 40-byte nodes are replaced on the device by 32-byte
+    # internal nodes plus 32-byte rope records per leaf (68 B per internal node)
+    _, nodes, side = blob_volumes
+    vol = ctx.upload_svo(nodes, side)
+    n_internal = int(np.sum(nodes[:, 9] < 0x80000000))
+    n_leaves = nodes.shape[0] - n_internal
+    assert vol.info()["device_bytes"] == n_internal * 68 + n_leaves * 32
+
+
+@pytest.mark.parametrize("trav", ("svo-df", "svo-naive", "esvo", "svo-rope"))
+def test_parity_tree_with_inconsistent_depth_fields(ctx, blob_volumes, trav):
+    # svo-df reads a node's depth field when it pops back to it; where the
+    # fields disagree with the tree the literal traversal (not the masked
+    # one) must run, and give the reference's (different) picture
+    import xenodon_gb300 as xg
+    _, nodes, side = blob_volumes
+    bad = nodes.copy()
+    internal = np.nonzero(bad[:, 9] < 0x80000000)[0]
+    bad[internal[bad[internal, 9] == 2][:3], 9] = 3
+    p, v = _params_pair(xg, 96, 64)
+    check_parity(ctx, trav, CAMS["oblique"], p, v, nodes=bad, side=side, label="inconsistent-depth")
+
+
+def test_full_size_ct_frame_matches_oracle_on_sampled_rows(ctx):
+    # the benchmark shape: 512x361x512 CT volume, 1920x1080, all five traversals;
+    # the oracle renders every 60th row of the same frame
+    import torch
+    import xenodon_gb300 as xg
+    from xenodon_gb300 import cameras, volumes
+    g = volumes.ct_shell(512, 361, 512, seed=1, device="cuda")
+    nodes, st = ctx.build_svo(g, "rope")
+    vg, vs_ = ctx.upload_grid(g), ctx.upload_svo(nodes, st["side"])
+    cam_t = cameras.ct_path()[37]
+    cam = xg.make_camera(*cam_t)
+    p = xg.make_params(1920, 1080, 10.0)
+    for trav in TRAV:
+        rgba, em, _ = ctx.render(vg if trav == "dda" else vs_, trav, cam, p, emission=True)
+        for y in range(7, 1080, 60):
+            v = oracle.make_view(1920, 1080, 10.0, output_offset=(0, y), output_extent=(1920, 1))
+            ref = oracle.render(trav, grid=g, nodes=nodes, camera=oracle.make_camera(*cam_t), view=v,
+                                want_loads=False)
+            assert np.abs(rgba[y].astype(int) - ref["rgba"][0].astype(int)).max() <= 1, (trav, y)
+            assert np.mean(em[y] == ref["emission"][0]) >= 0.999, (trav, y)
+    del torch
+
+
+@pytest.mark.parametrize("trav", TRAV)
+def test_emission_is_exactly_linear_in_the_coefficient(ctx, blob_volumes, trav):
+    # colour = trace * e * sqrt(...): doubling e doubles every emission bit for bit
+    import xenodon_gb300 as xg
+    g, nodes, side = blob_volumes
+    vol = ctx.upload_grid(g) if trav == "dda" else ctx.upload_svo(nodes, side)
+    cam = xg.make_camera(*CAMS["oblique"])
+    _, e1, _ = ctx.render(vol, trav, cam, xg.make_params(64, 48, 3.0), emission=True)
+    _, e2, _ = ctx.render(vol, trav, cam, xg.make_params(64, 48, 6.0), emission=True)
+    assert np.array_equal(e2, 2 * e1)
+    black, e0, _ = ctx.render(vol, trav, cam, xg.make_params(64, 48, 0.0), emission=True)
+    assert not np.any(e0) and np.all(black[..., :3] == 0) and np.all(black[..., 3] == 255)
+
+
+@pytest.mark.parametrize("trav", TRAV)
+def test_parity_empty_volume_and_degenerate_regions(ctx, trav):
+    import xenodon_gb300 as xg
+    g = np.zeros((16, 12, 20, 4), np.uint8)
+    g[..., 3] = 255
+    nodes, st = oracle.build_svo(g, "rope")
+    cases = [  # one pixel; a region of a display rectangle with a negative origin
+        dict(w=1, h=1, out_off=(0, 0), disp_off=(0, 0), disp_ext=None),
+        dict(w=17, h=5, out_off=(3, 9), disp_off=(-4, 2), disp_ext=(40, 30)),
+    ]
+    for c in cases:
+        p, v = _params_pair(xg, c["w"], c["h"], out_off=c["out_off"], out_ext=(c["w"], c["h"]),
+                            disp_off=c["disp_off"], disp_ext=c["disp_ext"])
+        check_parity(ctx, trav, CAMS["inside"], p, v, grid=g, nodes=nodes, side=st["side"], label="empty")

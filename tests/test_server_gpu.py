@@ -1,0 +1,112 @@
+"""The render server: continuous batching with resident volumes, LRU eviction
+and HBM-budget admission.  Every result must equal the same request rendered
+alone (bit for bit: the arithmetic is identical)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def volumes_data():
+    from xenodon_gb300 import volumes
+    g0 = volumes.blobs(64, seed=11)
+    g1 = volumes.ct_shell(48, 34, 48, seed=1, device="cpu")
+    n0, s0 = oracle.build_svo(g0, "rope")
+    n1, s1 = oracle.build_svo(g1, "rope")
+    return {1: ("grid", g0), 2: ("svo", (n0, s0["side"])), 3: ("grid", g1), 4: ("svo", (n1, s1["side"]))}
+
+
+def _requests(xg, rng, k):
+    cams = [((0, 0, -0.8660254), (0, 1, 0), (0.5, 0.5, 2.5)),
+            ((0.35, -0.2, -0.91), (0.0, 0.976, -0.215), (0.2, 0.8, 2.0)),
+            ((0.6, 0.3, 0.74), (-0.2, 0.95, 0.0), (0.45, 0.55, 0.5))]
+    sizes = [(64, 64), (31, 17), (120, 40), (8, 8)]
+    out = []
+    for i in range(k):
+        vid = int(rng.integers(1, 5))
+        trav = "dda" if vid in (1, 3) else ["svo-naive", "esvo", "svo-df", "svo-rope"][int(rng.integers(0, 4))]
+        w, h = sizes[int(rng.integers(0, len(sizes)))]
+        out.append((vid, trav, cams[int(rng.integers(0, 3))], xg.make_params(w, h, 10.0)))
+    return out
+
+
+def _alone(ctx, vols, req):
+    import xenodon_gb300 as xg
+    vid, trav, cam, p = req
+    rgba, _, _ = ctx.render(vols[vid], trav, xg.make_camera(*cam), p)
+    return rgba
+
+
+def _register(server, ctx, volumes_data):
+    handles = {}
+    for vid, (kind, data) in volumes_data.items():
+        if kind == "grid":
+            server.add_grid(vid, data)
+            handles[vid] = ctx.upload_grid(data)
+        else:
+            server.add_svo(vid, data[0], data[1])
+            handles[vid] = ctx.upload_svo(data[0], data[1])
+    return handles
+
+
+def test_results_equal_alone_and_in_the_mix(ctx, volumes_data):
+    import xenodon_gb300 as xg
+    rng = np.random.default_rng(3)
+    with xg.Server(ctx, max_batch_jobs=16, streams=2) as server:
+        vols = _register(server, ctx, volumes_data)
+        reqs = _requests(xg, rng, 60)
+        tickets = [server.submit(vid, trav, xg.make_camera(*cam), p) for vid, trav, cam, p in reqs]
+        for t, req in zip(tickets, reqs):
+            rgba, lat = server.wait(t, timeout=60)
+            assert lat > 0
+            assert np.array_equal(rgba, _alone(ctx, vols, req)), req[:2]
+        st = server.stats()
+        assert st["completed"] == 60 and st["failed"] == 0
+        assert st["batches"] < 60  # requests were batched together
+        assert 0 < st["p50_ms"] <= st["p99_ms"] <= st["max_ms"]
+        assert st["mrays_per_s"] > 0
+
+
+def test_lru_eviction_under_a_tight_budget(ctx, volumes_data):
+    import xenodon_gb300 as xg
+    # room for the largest volume plus frames, not for all four volumes
+    sizes = {vid: (d.nbytes if k == "grid" else d[0].shape[0] * 72) for vid, (k, d) in volumes_data.items()}
+    budget = max(sizes.values()) + 4 * 120 * 64 * 4 + (1 << 20)
+    assert budget < sum(sizes.values())
+    rng = np.random.default_rng(5)
+    with xg.Server(ctx, hbm_budget=budget, max_batch_jobs=4, streams=1) as server:
+        vols = _register(server, ctx, volumes_data)
+        reqs = _requests(xg, rng, 24)
+        results = []
+        for vid, trav, cam, p in reqs:  # one at a time: every switch of volume forces an upload
+            t = server.submit(vid, trav, xg.make_camera(*cam), p)
+            results.append(server.wait(t, timeout=60)[0])
+        for r, req in zip(results, reqs):
+            assert np.array_equal(r, _alone(ctx, vols, req))
+        st = server.stats()
+        assert st["evictions"] > 0 and st["uploads"] > 4
+        assert st["hbm_used"] <= budget
+
+
+def test_server_rejects_bad_requests(ctx, volumes_data):
+    import xenodon_gb300 as xg
+    with xg.Server(ctx, hbm_budget=1 << 20) as server:
+        kind, g = volumes_data[1]
+        server.add_grid(1, g)
+        cam = xg.make_camera((0, 0, 1), (0, 1, 0), (0.5, 0.5, -1))
+        with pytest.raises(xg.XenodonError):
+            server.submit(9, "dda", cam, xg.make_params(8, 8))  # unknown volume
+        with pytest.raises(xg.XenodonError):
+            server.submit(1, "esvo", cam, xg.make_params(8, 8))  # traversal does not fit the volume
+        with pytest.raises(xg.XenodonError) as e:
+            server.submit(1, "dda", cam, xg.make_params(1024, 1024))  # frame larger than the budget
+        assert e.value.code == xg.XN_ERR_BUDGET
+        # the volume (1 MiB budget, 1 MiB grid + frame) can never fit: the request fails, not hangs
+        t = server.submit(1, "dda", cam, xg.make_params(8, 8))
+        with pytest.raises(xg.XenodonError):
+            server.wait(t, timeout=30)

@@ -30,8 +30,11 @@ XN_ERR_BUDGET, XN_ERR_RAY_LIMIT, XN_ERR_IO, XN_ERR_STATE = -5, -6, -7, -8
 # Every symbol include/xenodon.h declares.
 EXPORTS = (
     "xn_create", "xn_destroy", "xn_last_error", "xn_abi_version", "xn_ctx_memory",
-    "xn_volume_upload_grid", "xn_volume_upload_svo", "xn_volume_release", "xn_volume_info_get",
+    "xn_volume_upload_grid", "xn_volume_upload_grid_device", "xn_build_svo_volume", "xn_volume_upload_svo", "xn_volume_release", "xn_volume_info_get",
     "xn_render", "xn_render_device", "xn_ray_errors", "xn_build_svo", "xn_build_svo_static", "xn_free",
+    "xn_render_batch", "xn_autotune_batch", "xn_batch_graph_create", "xn_batch_graph_launch",
+    "xn_batch_graph_destroy", "xn_server_create", "xn_server_destroy", "xn_server_add_grid",
+    "xn_server_add_svo", "xn_server_submit", "xn_server_wait", "xn_server_stats",
     "xn_svo_load", "xn_svo_save", "xn_tiff_load", "xn_tiff_save", "xn_png_save",
 )
 
@@ -62,6 +65,33 @@ class VolumeInfo(ctypes.Structure):
                 ("n_nodes", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64), ("has_ropes", ctypes.c_int)]
 
 
+class Job(ctypes.Structure):
+    _fields_ = [("volume", ctypes.c_void_p), ("traversal", ctypes.c_int), ("camera", Camera),
+                ("params", Params), ("d_rgba", ctypes.c_void_p)]
+
+
+class BatchConfig(ctypes.Structure):
+    _fields_ = [("tile_width", ctypes.c_uint32), ("block_threads", ctypes.c_uint32),
+                ("blocks_per_sm", ctypes.c_uint32), ("chunk", ctypes.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget", ctypes.c_uint64), ("max_batch_jobs", ctypes.c_int), ("streams", ctypes.c_int)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64), ("batches", ctypes.c_uint64),
+                ("uploads", ctypes.c_uint64), ("evictions", ctypes.c_uint64), ("rays", ctypes.c_uint64),
+                ("hbm_used", ctypes.c_uint64), ("mean_batch", ctypes.c_double), ("p50_ms", ctypes.c_double),
+                ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("mrays_per_s", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class BuildStats(ctypes.Structure):
     _fields_ = [("total_leaves", ctypes.c_uint64), ("unique_leaves", ctypes.c_uint64),
                 ("total_nodes", ctypes.c_uint64), ("depth", ctypes.c_uint64),
@@ -90,6 +120,8 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "xn_ctx_memory": (i32, [vp, P(u64), P(u64)]),
         "xn_volume_upload_grid": (i32, [vp, vp, u32, u32, u32, P(vp)]),
         "xn_volume_upload_svo": (i32, [vp, vp, u64, u64, P(vp)]),
+        "xn_volume_upload_grid_device": (i32, [vp, vp, u32, u32, u32, P(vp)]),
+        "xn_build_svo_volume": (i32, [vp, vp, u32, u32, u32, i32, i32, ctypes.c_double, P(vp), P(BuildStats)]),
         "xn_volume_release": (i32, [vp]),
         "xn_volume_info_get": (i32, [vp, P(VolumeInfo)]),
         "xn_render": (i32, [vp, vp, i32, P(Camera), P(Params), vp, vp, P(ctypes.c_float)]),
@@ -98,6 +130,18 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "xn_build_svo": (i32, [vp, vp, u32, u32, u32, i32, i32, ctypes.c_double, P(P(u32)), P(BuildStats)]),
         "xn_build_svo_static": (i32, [vp, u32, u32, u32, i32, i32, ctypes.c_double, vp, u64, P(BuildStats), vp]),
         "xn_free": (None, [vp]),
+        "xn_render_batch": (i32, [vp, P(Job), i32, P(BatchConfig), vp]),
+        "xn_autotune_batch": (i32, [vp, P(Job), i32, vp, P(BatchConfig), P(ctypes.c_float)]),
+        "xn_batch_graph_create": (i32, [vp, i32, P(BatchConfig), vp, P(vp)]),
+        "xn_batch_graph_launch": (i32, [vp, P(Job), i32]),
+        "xn_batch_graph_destroy": (i32, [vp]),
+        "xn_server_create": (i32, [vp, P(ServerConfig), P(vp)]),
+        "xn_server_destroy": (i32, [vp]),
+        "xn_server_add_grid": (i32, [vp, u32, vp, u32, u32, u32]),
+        "xn_server_add_svo": (i32, [vp, u32, vp, u64, u64]),
+        "xn_server_submit": (i32, [vp, u32, i32, P(Camera), P(Params), vp, P(u64)]),
+        "xn_server_wait": (i32, [vp, u64, ctypes.c_double, P(ctypes.c_double)]),
+        "xn_server_stats": (i32, [vp, P(ServerStats)]),
         "xn_svo_load": (i32, [ctypes.c_char_p, P(P(u32)), P(u64), P(u64)]),
         "xn_svo_save": (i32, [ctypes.c_char_p, vp, u64, u64]),
         "xn_tiff_load": (i32, [ctypes.c_char_p, P(P(ctypes.c_uint8)), P(u32 * 3)]),
@@ -210,6 +254,20 @@ class Context:
                                               ctypes.byref(h)))
         return Volume(self, h)
 
+    def upload_grid_device(self, d_rgba: int, dims) -> Volume:
+        """Grid already on the device: d_rgba points at dx*dy*dz packed RGBA8 texels; dims = (dx, dy, dz)."""
+        h = ctypes.c_void_p()
+        _check(self.lib.xn_volume_upload_grid_device(self.handle, d_rgba, dims[0], dims[1], dims[2], ctypes.byref(h)))
+        return Volume(self, h)
+
+    def build_svo_volume(self, d_rgba: int, dims, svo_type="rope", heuristic="chan-diff", threshold=0.0):
+        """Octree of a device grid, built and kept on the device.  Returns (Volume, stats)."""
+        h = ctypes.c_void_p()
+        st = BuildStats()
+        _check(self.lib.xn_build_svo_volume(self.handle, d_rgba, dims[0], dims[1], dims[2], SVO_TYPES[svo_type],
+                                            HEURISTICS[heuristic], float(threshold), ctypes.byref(h), ctypes.byref(st)))
+        return Volume(self, h), {f: int(getattr(st, f)) for f, _ in BuildStats._fields_}
+
     def upload_svo(self, nodes: np.ndarray, side: int) -> Volume:
         """nodes: uint32 (n, 10) in the reference layout."""
         n = np.ascontiguousarray(nodes, dtype=np.uint32).reshape(-1, 10)
@@ -245,6 +303,27 @@ class Context:
         _check(self.lib.xn_render_device(self.handle, vol.handle, _traversal(traversal), ctypes.byref(camera),
                                          ctypes.byref(params), d_rgba, d_emission, d_loads, stream))
 
+    def make_jobs(self, specs) -> ctypes.Array:
+        """specs: iterable of (volume, traversal, camera, params, device pointer)."""
+        specs = list(specs)
+        arr = (Job * max(1, len(specs)))()
+        for i, (vol, trav, cam, params, ptr) in enumerate(specs):
+            arr[i] = Job(vol.handle, _traversal(trav), cam, params, ptr)
+        return arr
+
+    def render_batch(self, jobs, n: int, config: BatchConfig | None = None, stream: int | None = None) -> None:
+        """One persistent launch over n jobs (see make_jobs); asynchronous on `stream`."""
+        _check(self.lib.xn_render_batch(self.handle, jobs, n, ctypes.byref(config) if config else None, stream))
+
+    def autotune_batch(self, jobs, n: int, stream: int | None = None) -> tuple[BatchConfig, float]:
+        best = BatchConfig()
+        ms = ctypes.c_float()
+        _check(self.lib.xn_autotune_batch(self.handle, jobs, n, stream, ctypes.byref(best), ctypes.byref(ms)))
+        return best, ms.value
+
+    def batch_graph(self, capacity: int, config: BatchConfig | None = None, stream: int | None = None):
+        return BatchGraph(self, capacity, config, stream)
+
     def ray_errors(self, reset: bool = True) -> int:
         bits = ctypes.c_uint32()
         _check(self.lib.xn_ray_errors(self.handle, ctypes.byref(bits), int(reset)))
@@ -264,6 +343,87 @@ class Context:
         finally:
             self.lib.xn_free(out)
         return arr, {f: int(getattr(st, f)) for f, _ in BuildStats._fields_}
+
+
+class BatchGraph:
+    """xn_batch_graph: a captured batch launch replayed per batch."""
+
+    def __init__(self, ctx: Context, capacity: int, config: BatchConfig | None, stream: int | None):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        _check(ctx.lib.xn_batch_graph_create(ctx.handle, capacity, ctypes.byref(config) if config else None,
+                                             stream, ctypes.byref(h)))
+        self.handle = h
+
+    def launch(self, jobs, n: int) -> None:
+        _check(self.ctx.lib.xn_batch_graph_launch(self.handle, jobs, n))
+
+    def close(self) -> None:
+        if self.handle:
+            self.ctx.lib.xn_batch_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """xn_server: continuous batching of render requests on one context."""
+
+    def __init__(self, ctx: Context, hbm_budget: int = 0, max_batch_jobs: int = 256, streams: int = 2):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        cfg = ServerConfig(hbm_budget, max_batch_jobs, streams)
+        h = ctypes.c_void_p()
+        _check(self.lib.xn_server_create(ctx.handle, ctypes.byref(cfg), ctypes.byref(h)))
+        self.handle = h
+        self._outputs = {}
+
+    def add_grid(self, volume_id: int, grid: np.ndarray) -> None:
+        g = np.ascontiguousarray(grid, dtype=np.uint8)
+        _check(self.lib.xn_server_add_grid(self.handle, volume_id, g.ctypes.data, g.shape[2], g.shape[1], g.shape[0]))
+
+    def add_svo(self, volume_id: int, nodes: np.ndarray, side: int) -> None:
+        n = np.ascontiguousarray(nodes, dtype=np.uint32).reshape(-1, 10)
+        _check(self.lib.xn_server_add_svo(self.handle, volume_id, n.ctypes.data, n.shape[0], int(side)))
+
+    def submit(self, volume_id: int, traversal, camera: Camera, params: Params, out: np.ndarray | None = None) -> int:
+        w, h = params.output_region.width, params.output_region.height
+        if out is None:
+            out = np.empty((h, w, 4), np.uint8)
+        t = ctypes.c_uint64()
+        _check(self.lib.xn_server_submit(self.handle, volume_id, _traversal(traversal), ctypes.byref(camera),
+                                         ctypes.byref(params), out.ctypes.data, ctypes.byref(t)))
+        self._outputs[t.value] = out
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = -1.0):
+        """Returns (rgba, latency_ms)."""
+        lat = ctypes.c_double()
+        try:
+            _check(self.lib.xn_server_wait(self.handle, ticket, float(timeout), ctypes.byref(lat)))
+        finally:
+            out = self._outputs.pop(ticket, None)
+        return out, lat.value
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(self.lib.xn_server_stats(self.handle, ctypes.byref(st)))
+        return st.as_dict()
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.xn_server_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def svo_load(path) -> tuple[np.ndarray, int]:

@@ -1,0 +1,307 @@
+// Batched rendering: job tables, the persistent launch, CUDA-graph replay and
+// the launch-shape autotuner.  (No counterpart in the reference, which renders
+// one frame per dispatch, src/render/Renderer.cpp:74-89.)
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "../../include/xenodon.h"
+#include "xn_ctx.h"
+#include "xn_internal.h"
+
+namespace xn {
+
+int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_params* p, RenderLaunch& L);
+
+namespace {
+
+uint32_t traversal_mask(const xn_job* jobs, int n) {
+    uint32_t m = 0;
+    for (int i = 0; i < n; ++i) m |= 1u << (jobs[i].traversal & 7);
+    return m;
+}
+
+int check_config(const xn_batch_config& c) {
+    if (c.tile_width != 4 && c.tile_width != 8 && c.tile_width != 16 && c.tile_width != 32)
+        return fail(XN_ERR_ARG, "batch: tile_width must be 4, 8, 16 or 32");
+    if (c.block_threads == 0 || c.block_threads % 32 || c.block_threads > 1024)
+        return fail(XN_ERR_ARG, "batch: block_threads must be a multiple of 32 up to 1024");
+    if (c.chunk == 0) return fail(XN_ERR_ARG, "batch: chunk must be >= 1");
+    return XN_OK;
+}
+
+// Builds header + jobs into `table`; returns the byte size.
+int fill_table(Ctx* c, const xn_job* jobs, int n, uint32_t tile_w, void* table, uint64_t capacity_bytes,
+               uint64_t* bytes_out) {
+    const uint64_t need = sizeof(BatchHeader) + (uint64_t)n * sizeof(BatchJob);
+    if (need > capacity_bytes) return fail(XN_ERR_ARG, "batch: %d jobs exceed the job table capacity", n);
+    BatchHeader* h = static_cast<BatchHeader*>(table);
+    BatchJob* out = reinterpret_cast<BatchJob*>(h + 1);
+    const uint32_t tile_h = 32 / tile_w;
+    unsigned long long tiles = 0;
+    for (int i = 0; i < n; ++i) {
+        const xn_job& j = jobs[i];
+        if (!j.volume || !j.d_rgba) return fail(XN_ERR_ARG, "batch: job %d has no volume or output", i);
+        const Volume* v = reinterpret_cast<const Volume*>(j.volume);
+        if (v->ctx != c) return fail(XN_ERR_ARG, "batch: job %d uses a volume of another context", i);
+        RenderLaunch L;
+        int r = make_launch(v, j.traversal, &j.camera, &j.params, L);
+        if (r) return r;
+        L.d_rgba = j.d_rgba;
+        out[i] = make_batch_job(L);
+        out[i].tiles_x = (L.out_w + tile_w - 1) / tile_w;
+        out[i].tiles_y = (L.out_h + tile_h - 1) / tile_h;
+        out[i].tile_begin = tiles;
+        tiles += (unsigned long long)out[i].tiles_x * out[i].tiles_y;
+    }
+    h->n_jobs = (uint32_t)n;
+    h->pad = 0;
+    h->total_tiles = tiles;
+    *bytes_out = need;
+    return XN_OK;
+}
+
+uint32_t resident_blocks(Ctx* c, const xn_batch_config& cfg) {
+    int per_sm = batch_kernel_blocks_per_sm(cfg.tile_width, cfg.block_threads);
+    if (per_sm < 1) per_sm = 1;
+    if (cfg.blocks_per_sm && (int)cfg.blocks_per_sm < per_sm) per_sm = (int)cfg.blocks_per_sm;
+    return (uint32_t)per_sm * (uint32_t)c->sm_count();
+}
+
+xn_batch_config default_config() { return xn_batch_config{8, 128, 0, 1}; }
+
+// Job-table buffers of a context for xn_render_batch.
+int ensure_batch_buffers(Ctx* c, uint64_t bytes) {
+    if (c->batch_host_bytes < bytes) {
+        if (c->batch_host) {
+            cudaEventSynchronize(c->batch_copied);
+            cudaFreeHost(c->batch_host);
+            c->batch_host = nullptr;
+            c->batch_host_bytes = 0;
+        }
+        if (cudaHostAlloc(&c->batch_host, bytes, cudaHostAllocDefault) != cudaSuccess)
+            return fail(XN_ERR_NOMEM, "batch: pinned job table");
+        c->batch_host_bytes = bytes;
+    }
+    if (c->batch_table.bytes < bytes) {
+        cudaDeviceSynchronize();  // the previous table may still be read
+        int r = c->ensure_buffer(c->batch_table, bytes, "batch: job table");
+        if (r) return r;
+    }
+    if (!c->batch_queue.ptr) {
+        int r = c->ensure_buffer(c->batch_queue, 64, "batch: work queue");
+        if (r) return r;
+    }
+    if (!c->batch_copied && cudaEventCreateWithFlags(&c->batch_copied, cudaEventDisableTiming) != cudaSuccess)
+        return fail(XN_ERR_CUDA, "batch: event");
+    return XN_OK;
+}
+
+int render_batch_locked(Ctx* c, const xn_job* jobs, int n, const xn_batch_config& cfg, cudaStream_t s) {
+    const uint64_t cap = sizeof(BatchHeader) + (uint64_t)n * sizeof(BatchJob);
+    int r = ensure_batch_buffers(c, cap);
+    if (r) return r;
+    cudaEventSynchronize(c->batch_copied);  // the staging table of the previous batch was copied
+    uint64_t bytes = 0;
+    if ((r = fill_table(c, jobs, n, cfg.tile_width, c->batch_host, c->batch_host_bytes, &bytes))) return r;
+    cudaError_t e = cudaMemcpyAsync(c->batch_table.ptr, c->batch_host, bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaEventRecord(c->batch_copied, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->batch_queue.ptr, 0, 8, s);
+    if (e == cudaSuccess)
+        e = launch_batch(c->batch_table.ptr, static_cast<unsigned long long*>(c->batch_queue.ptr), c->d_err,
+                         cfg.tile_width, cfg.block_threads, resident_blocks(c, cfg), cfg.chunk, s);
+    return e == cudaSuccess ? XN_OK : cuda_fail(e, "xn_render_batch");
+}
+
+}  // namespace
+
+int Ctx::sm_count() {
+    if (sms <= 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || v <= 0) v = 1;
+        sms = v;
+    }
+    return sms;
+}
+
+}  // namespace xn
+
+using namespace xn;
+
+XN_API int xn_render_batch(xn_ctx* h, const xn_job* jobs, int n, const xn_batch_config* cfg, void* stream) {
+    if (!h || (!jobs && n)) return fail(XN_ERR_ARG, "xn_render_batch: NULL argument");
+    if (n <= 0) return XN_OK;
+    Ctx* c = reinterpret_cast<Ctx*>(h);
+    std::lock_guard<std::mutex> lk(c->mu);
+    int r = c->activate();
+    if (r) return r;
+    xn_batch_config k = default_config();
+    if (cfg) k = *cfg;
+    else if (c->tuned_valid[traversal_mask(jobs, n)]) k = c->tuned[traversal_mask(jobs, n)];
+    if ((r = check_config(k))) return r;
+    return render_batch_locked(c, jobs, n, k, static_cast<cudaStream_t>(stream));
+}
+
+XN_API int xn_autotune_batch(xn_ctx* h, const xn_job* jobs, int n, void* stream, xn_batch_config* best,
+                             float* best_ms) {
+    if (!h || !jobs || n <= 0) return fail(XN_ERR_ARG, "xn_autotune_batch: no jobs");
+    Ctx* c = reinterpret_cast<Ctx*>(h);
+    std::lock_guard<std::mutex> lk(c->mu);
+    int r = c->activate();
+    if (r) return r;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        return fail(XN_ERR_CUDA, "xn_autotune_batch: events");
+    const uint32_t tiles[] = {4, 8, 16, 32};
+    const uint32_t threads[] = {64, 128, 256};
+    const uint32_t chunks[] = {1, 2, 4};
+    xn_batch_config winner = default_config();
+    float winner_ms = 3.4e38f;
+    for (uint32_t tw : tiles)
+        for (uint32_t bt : threads)
+            for (uint32_t ch : chunks) {
+                xn_batch_config k{tw, bt, 0, ch};
+                if ((r = render_batch_locked(c, jobs, n, k, s))) break;  // warm-up
+                float total = 0;
+                const int reps = 3;
+                for (int i = 0; i < reps && !r; ++i) {
+                    cudaEventRecord(e0, s);
+                    r = render_batch_locked(c, jobs, n, k, s);
+                    cudaEventRecord(e1, s);
+                    float ms = 0;
+                    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+                        r = fail(XN_ERR_CUDA, "xn_autotune_batch: timing");
+                    total += ms;
+                }
+                if (r) break;
+                if (total / reps < winner_ms) {
+                    winner_ms = total / reps;
+                    winner = k;
+                }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (r) return r;
+    const uint32_t m = traversal_mask(jobs, n);
+    c->tuned[m] = winner;
+    c->tuned_valid[m] = 1;
+    if (best) *best = winner;
+    if (best_ms) *best_ms = winner_ms;
+    return XN_OK;
+}
+
+// ------------------------------------------------------------------ graphs
+
+struct xn_batch_graph {
+    Ctx* ctx;
+    cudaStream_t stream;
+    xn_batch_config cfg;
+    int capacity;
+    uint64_t table_bytes;
+    struct Slot {
+        void* host = nullptr;
+        void* dev = nullptr;
+        unsigned long long* queue = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        cudaEvent_t done = nullptr;
+        bool pending = false;
+    } slot[2];
+    int next = 0;
+};
+
+namespace {
+
+void destroy_graph(xn_batch_graph* g) {
+    Ctx* c = g->ctx;
+    for (auto& s : g->slot) {
+        if (s.done) {
+            cudaEventSynchronize(s.done);
+            cudaEventDestroy(s.done);
+        }
+        if (s.exec) cudaGraphExecDestroy(s.exec);
+        if (s.host) cudaFreeHost(s.host);
+        c->device_free(s.dev, g->table_bytes);
+        c->device_free(s.queue, 64);
+    }
+    delete g;
+}
+
+}  // namespace
+
+XN_API int xn_batch_graph_create(xn_ctx* h, int capacity, const xn_batch_config* cfg, void* stream,
+                                 xn_batch_graph** out) {
+    if (!h || !out || capacity <= 0) return fail(XN_ERR_ARG, "xn_batch_graph_create: bad argument");
+    *out = nullptr;
+    Ctx* c = reinterpret_cast<Ctx*>(h);
+    std::lock_guard<std::mutex> lk(c->mu);
+    int r = c->activate();
+    if (r) return r;
+    xn_batch_graph* g = new (std::nothrow) xn_batch_graph();
+    if (!g) return fail(XN_ERR_NOMEM, "xn_batch_graph_create: out of host memory");
+    g->ctx = c;
+    g->stream = static_cast<cudaStream_t>(stream);
+    g->cfg = cfg ? *cfg : default_config();
+    g->capacity = capacity;
+    g->table_bytes = sizeof(BatchHeader) + (uint64_t)capacity * sizeof(BatchJob);
+    if ((r = check_config(g->cfg))) {
+        delete g;
+        return r;
+    }
+    const uint32_t blocks = resident_blocks(c, g->cfg);
+    cudaStream_t cap = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    for (auto& sl : g->slot) {
+        if (e != cudaSuccess || r) break;
+        if ((e = cudaHostAlloc(&sl.host, g->table_bytes, cudaHostAllocDefault)) != cudaSuccess) break;
+        std::memset(sl.host, 0, sizeof(BatchHeader));
+        if ((r = c->device_alloc(&sl.dev, g->table_bytes, "xn_batch_graph_create: job table"))) break;
+        if ((r = c->device_alloc(reinterpret_cast<void**>(&sl.queue), 64, "xn_batch_graph_create: queue"))) break;
+        if ((e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming)) != cudaSuccess) break;
+        // capture: table upload, queue reset, persistent kernel
+        if ((e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
+        cudaMemcpyAsync(sl.dev, sl.host, g->table_bytes, cudaMemcpyHostToDevice, cap);
+        cudaMemsetAsync(sl.queue, 0, 8, cap);
+        launch_batch(sl.dev, sl.queue, c->d_err, g->cfg.tile_width, g->cfg.block_threads, blocks, g->cfg.chunk, cap);
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamEndCapture(cap, &graph);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&sl.exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+    }
+    if (cap) cudaStreamDestroy(cap);
+    if (e != cudaSuccess || r) {
+        destroy_graph(g);
+        return r ? r : cuda_fail(e, "xn_batch_graph_create");
+    }
+    *out = g;
+    return XN_OK;
+}
+
+XN_API int xn_batch_graph_launch(xn_batch_graph* g, const xn_job* jobs, int n) {
+    if (!g || (!jobs && n)) return fail(XN_ERR_ARG, "xn_batch_graph_launch: NULL argument");
+    if (n > g->capacity) return fail(XN_ERR_ARG, "xn_batch_graph_launch: %d jobs exceed the capacity %d", n, g->capacity);
+    Ctx* c = g->ctx;
+    std::lock_guard<std::mutex> lk(c->mu);
+    int r = c->activate();
+    if (r) return r;
+    auto& sl = g->slot[g->next];
+    if (sl.pending) cudaEventSynchronize(sl.done);  // this slot's previous batch has finished
+    uint64_t bytes = 0;
+    if ((r = fill_table(c, jobs, n, g->cfg.tile_width, sl.host, g->table_bytes, &bytes))) return r;
+    cudaError_t e = cudaGraphLaunch(sl.exec, g->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(sl.done, g->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "xn_batch_graph_launch");
+    sl.pending = true;
+    g->next ^= 1;
+    return XN_OK;
+}
+
+XN_API int xn_batch_graph_destroy(xn_batch_graph* g) {
+    if (!g) return XN_OK;
+    std::lock_guard<std::mutex> lk(g->ctx->mu);
+    g->ctx->activate();
+    destroy_graph(g);
+    return XN_OK;
+}

@@ -74,7 +74,15 @@ int Ctx::ensure_buffer(DeviceBuffer& b, uint64_t bytes, const char* what) {
     return r;
 }
 
-void Ctx::release_extra() {}
+void Ctx::release_extra() {
+    if (batch_copied) {
+        cudaEventSynchronize(batch_copied);
+        cudaEventDestroy(batch_copied);
+    }
+    if (batch_host) cudaFreeHost(batch_host);
+    device_free(batch_table.ptr, batch_table.bytes);
+    device_free(batch_queue.ptr, batch_queue.bytes);
+}
 
 int Ctx::activate() {
     cudaError_t e = cudaSetDevice(device);
@@ -170,9 +178,81 @@ __global__ void detect_ropes_kernel(const uint32_t* w, uint64_t n, uint32_t* any
 
 }  // namespace
 
-XN_API int xn_volume_upload_grid(xn_ctx* h, const uint8_t* rgba, uint32_t dx, uint32_t dy, uint32_t dz,
-                                 xn_volume** out) {
+namespace {
+
+__device__ __forceinline__ float unorm8_exact(uint32_t c) {
+    const float r = 1.0f / 255.0f;
+    float cf = __uint2float_rn(c);
+    float q0 = cf * r;
+    return fmaf(fmaf(-q0, 255.0f, cf), r, q0);
+}
+
+// Counts the bytes for which the texture unit's UNORM8 -> float differs from
+// byte/255 correctly rounded; all 256 fetches are in range.
+__global__ void tex_unorm_check_kernel(cudaTextureObject_t t, unsigned* mismatches) {
+    const unsigned i = threadIdx.x;
+    float4 v = tex3D<float4>(t, i + 0.5f, 0.5f, 0.5f);
+    const float e = unorm8_exact(i), f = unorm8_exact(255 - i);
+    unsigned bad = (v.x != e) + (v.y != f) + (v.z != e) + (v.w != f);
+    if (bad) atomicAdd(mismatches, bad);
+}
+
+cudaTextureObject_t make_texture(cudaArray_t a, bool normalized) {
+    cudaResourceDesc rd = {};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = a;
+    cudaTextureDesc td = {};
+    td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeBorder;  // border colour 0
+    td.filterMode = cudaFilterModePoint;
+    td.readMode = normalized ? cudaReadModeNormalizedFloat : cudaReadModeElementType;
+    td.normalizedCoords = 0;
+    cudaTextureObject_t t = 0;
+    if (cudaCreateTextureObject(&t, &rd, &td, nullptr) != cudaSuccess) return 0;
+    return t;
+}
+
+// Whether this device's texture unit returns exactly byte/255 (decided once
+// per context by comparing all 256 values; otherwise the kernels convert the
+// raw bytes themselves).
+int texture_unorm_exact(Ctx* c) {
+    if (c->tex_norm_exact >= 0) return c->tex_norm_exact;
+    c->tex_norm_exact = 0;
+    cudaChannelFormatDesc d = cudaCreateChannelDesc<uchar4>();
+    cudaArray_t a = nullptr;
+    if (cudaMalloc3DArray(&a, &d, make_cudaExtent(256, 1, 1)) != cudaSuccess) return 0;
+    uchar4 h[256];
+    for (int i = 0; i < 256; ++i) h[i] = make_uchar4(i, 255 - i, i, 255 - i);
+    cudaMemcpy3DParms p = {};
+    p.srcPtr = make_cudaPitchedPtr(h, sizeof h, 256, 1);
+    p.dstArray = a;
+    p.extent = make_cudaExtent(256, 1, 1);
+    p.kind = cudaMemcpyHostToDevice;
+    unsigned* bad = nullptr;
+    cudaTextureObject_t t = 0;
+    unsigned hb = 1;
+    if (cudaMemcpy3DAsync(&p, c->stream) == cudaSuccess && (t = make_texture(a, true)) != 0 &&
+        cudaMallocAsync(reinterpret_cast<void**>(&bad), 4, c->stream) == cudaSuccess &&
+        cudaMemsetAsync(bad, 0, 4, c->stream) == cudaSuccess) {
+        tex_unorm_check_kernel<<<1, 256, 0, c->stream>>>(t, bad);
+        if (cudaMemcpyAsync(&hb, bad, 4, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) hb = 1;
+        if (cudaStreamSynchronize(c->stream) != cudaSuccess) hb = 1;
+    }
+    if (bad) cudaFreeAsync(bad, c->stream);
+    cudaStreamSynchronize(c->stream);
+    if (t) cudaDestroyTextureObject(t);
+    cudaFreeArray(a);
+    c->tex_norm_exact = hb == 0 ? 1 : 0;
+    return c->tex_norm_exact;
+}
+
+}  // namespace
+
+namespace {
+
+int upload_grid(xn_ctx* h, const uint8_t* rgba, bool from_device, uint32_t dx, uint32_t dy, uint32_t dz,
+                xn_volume** out) {
     if (!h || !rgba || !out) return fail(XN_ERR_ARG, "xn_volume_upload_grid: NULL argument");
+    const cudaMemcpyKind kind = from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     *out = nullptr;
     if (!dx || !dy || !dz) return fail(XN_ERR_ARG, "xn_volume_upload_grid: empty grid %ux%ux%u", dx, dy, dz);
     if ((uint64_t)dx + dy + dz > (1ull << 30)) return fail(XN_ERR_ARG, "xn_volume_upload_grid: grid too large");
@@ -187,10 +267,58 @@ XN_API int xn_volume_upload_grid(xn_ctx* h, const uint8_t* rgba, uint32_t dx, ui
     v->dim[0] = dx;
     v->dim[1] = dy;
     v->dim[2] = dz;
-    v->bytes = (uint64_t)dx * dy * dz * 4;
+    const uint64_t bytes = (uint64_t)dx * dy * dz * 4;
+    // texture form unless XN_GRID_LAYOUT=linear or the device's 3D texture
+    // limits are exceeded
+    const char* lay = std::getenv("XN_GRID_LAYOUT");
+    bool use_tex = !(lay && std::strcmp(lay, "linear") == 0);
+    if (use_tex) {
+        cudaDeviceProp prop;
+        if (cudaGetDeviceProperties(&prop, c->device) != cudaSuccess || (int)dx > prop.maxTexture3D[0] ||
+            (int)dy > prop.maxTexture3D[1] || (int)dz > prop.maxTexture3D[2])
+            use_tex = false;
+    }
+    cudaError_t e = cudaSuccess;
+    if (use_tex) {
+        const bool norm = texture_unorm_exact(c) == 1;
+        if (c->budget && c->used.load() + bytes > c->budget) {
+            delete v;
+            return fail(XN_ERR_BUDGET, "xn_volume_upload_grid: %llu bytes exceed the HBM budget",
+                        (unsigned long long)bytes);
+        }
+        cudaChannelFormatDesc d = cudaCreateChannelDesc<uchar4>();
+        e = cudaMalloc3DArray(&v->array, &d, make_cudaExtent(dx, dy, dz));
+        if (e != cudaSuccess) {
+            delete v;
+            return cuda_fail(e, "xn_volume_upload_grid: array");
+        }
+        v->array_bytes = bytes;
+        c->used += bytes;
+        cudaMemcpy3DParms p = {};
+        p.srcPtr = make_cudaPitchedPtr(const_cast<uint8_t*>(rgba), (size_t)dx * 4, dx, dy);
+        p.dstArray = v->array;
+        p.extent = make_cudaExtent(dx, dy, dz);
+        p.kind = kind;
+        e = cudaMemcpy3DAsync(&p, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e == cudaSuccess) {
+            v->tex = make_texture(v->array, norm);
+            v->tex_normalized = norm;
+            if (!v->tex) e = cudaErrorInvalidValue;
+        }
+        if (e != cudaSuccess) {
+            cudaFreeArray(v->array);
+            c->used -= bytes;
+            delete v;
+            return cuda_fail(e, "xn_volume_upload_grid: texture");
+        }
+        *out = reinterpret_cast<xn_volume*>(v);
+        return XN_OK;
+    }
+    v->bytes = bytes;
     r = c->device_alloc(&v->data, v->bytes, "xn_volume_upload_grid");
     if (r) { delete v; return r; }
-    cudaError_t e = cudaMemcpyAsync(v->data, rgba, v->bytes, cudaMemcpyHostToDevice, c->stream);
+    e = cudaMemcpyAsync(v->data, rgba, v->bytes, kind, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) {
         c->device_free(v->data, v->bytes);
@@ -199,6 +327,18 @@ XN_API int xn_volume_upload_grid(xn_ctx* h, const uint8_t* rgba, uint32_t dx, ui
     }
     *out = reinterpret_cast<xn_volume*>(v);
     return XN_OK;
+}
+
+}  // namespace
+
+XN_API int xn_volume_upload_grid(xn_ctx* h, const uint8_t* rgba, uint32_t dx, uint32_t dy, uint32_t dz,
+                                 xn_volume** out) {
+    return upload_grid(h, rgba, false, dx, dy, dz, out);
+}
+
+XN_API int xn_volume_upload_grid_device(xn_ctx* h, const void* d_rgba, uint32_t dx, uint32_t dy, uint32_t dz,
+                                        xn_volume** out) {
+    return upload_grid(h, static_cast<const uint8_t*>(d_rgba), true, dx, dy, dz, out);
 }
 
 XN_API int xn_volume_upload_svo(xn_ctx* h, const uint32_t* nodes, uint64_t n_nodes, uint64_t side, xn_volume** out) {
@@ -242,6 +382,11 @@ XN_API int xn_volume_upload_svo(xn_ctx* h, const uint32_t* nodes, uint64_t n_nod
                     (unsigned long long)n_nodes);
     }
     v->has_ropes = hf[1] != 0;
+    if ((r = build_svo_layout(c, v))) {
+        c->device_free(v->data, v->bytes);
+        delete v;
+        return r;
+    }
     *out = reinterpret_cast<xn_volume*>(v);
     return XN_OK;
 }
@@ -254,6 +399,12 @@ XN_API int xn_volume_release(xn_volume* h) {
     c->activate();
     cudaStreamSynchronize(c->stream);
     c->device_free(v->data, v->bytes);
+    v->release_layout();
+    if (v->tex) cudaDestroyTextureObject(v->tex);
+    if (v->array) {
+        cudaFreeArray(v->array);
+        c->used -= v->array_bytes;
+    }
     delete v;
     return XN_OK;
 }
@@ -265,7 +416,7 @@ XN_API int xn_volume_info_get(const xn_volume* h, xn_volume_info* info) {
     for (int i = 0; i < 3; ++i) info->dim[i] = v->dim[i];
     info->side = v->side;
     info->n_nodes = v->n_nodes;
-    info->device_bytes = v->bytes;
+    info->device_bytes = v->bytes + v->array_bytes + (v->layout == XN_LAYOUT_COMPACT ? v->layout_bytes() : 0);
     info->has_ropes = v->has_ropes;
     return XN_OK;
 }
@@ -308,8 +459,16 @@ int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_p
     L.disp_h = p->display_region.height;
     if (v->kind == XN_VOLUME_GRID) {
         L.grid = v->data;
+        L.tex = v->tex;
+        L.tex_normalized = v->tex_normalized;
     } else {
         L.nodes = v->data;
+        L.layout = v->layout;
+        L.inner = v->inner;
+        L.rinner = v->rinner;
+        L.inner_depth = v->inner_depth;
+        L.leaves = v->leaves;
+        L.depth_consistent = v->depth_consistent;
     }
     for (int i = 0; i < 3; ++i) L.dim[i] = v->dim[i];
     return XN_OK;

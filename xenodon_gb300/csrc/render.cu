@@ -88,6 +88,72 @@ __device__ V3 trace_dda(const GridVol& g, V3 ro, V3 rd, uint32_t& loads, uint32_
     return total;
 }
 
+// Texture form of the grid: a 3D cudaArray (block-linear, so texels that
+// are near in 3D share cache lines) sampled with point filtering and a zero
+// border, which makes out-of-range reads 0 without a bounds check and leaves
+// the address arithmetic to the texture unit.  NORM: the unit returns
+// byte/255 (used when that conversion is exact, see xn_volume_upload_grid);
+// otherwise the raw bytes are converted with unorm8.
+template <bool NORM>
+__device__ __forceinline__ V3 tex_texel(cudaTextureObject_t t, float x, float y, float z) {
+    if (NORM) {
+        float4 v = tex3D<float4>(t, x, y, z);
+        return V3{v.x, v.y, v.z};
+    }
+    uchar4 v = tex3D<uchar4>(t, x, y, z);
+    return V3{unorm8(v.x), unorm8(v.y), unorm8(v.z)};
+}
+
+// resources/dda.comp:13-53 over the texture form; coordinates are kept as
+// texel centres (integers + 0.5, exact in float).
+template <bool COUNT, bool NORM>
+__device__ V3 trace_dda_tex(cudaTextureObject_t tex, uint32_t dx, uint32_t dy, uint32_t dz, V3 ro, V3 rd,
+                            uint32_t& loads, uint32_t& err) {
+    V3 rrd = vs(1.0f) / rd;
+    V3 bias = rrd * ro;
+    V3 box_min = -bias;
+    V3 md = v3((float)dx, (float)dy, (float)dz);
+    V3 box_max = md * rrd - bias;
+    float t_min = max_elem(vmin(box_min, box_max));
+    float t_max = min_elem(vmax(box_min, box_max));
+    if (t_min > t_max) return vs(0.0f);
+    t_min = fmaxf(t_min, 0.0f);
+    ro = ro + rd * t_min;
+    float px = (float)f2i(ro.x) + 0.5f, py = (float)f2i(ro.y) + 0.5f, pz = (float)f2i(ro.z) + 0.5f;
+    V3 t_delta = v3(fabsf(rrd.x), fabsf(rrd.y), fabsf(rrd.z));
+    V3 sgn = v3(gl_sign(rd.x), gl_sign(rd.y), gl_sign(rd.z));
+    V3 fr = (v3(floorf(ro.x), floorf(ro.y), floorf(ro.z)) - ro) + vs(0.5f);
+    V3 side = (sgn * fr + vs(0.5f)) * t_delta;
+    float t = 0.0f;
+    V3 total = vs(0.0f);
+    const float lim = t_max - t_min;
+    const uint32_t cap = 2u * (dx + dy + dz) + 64u;
+    uint32_t iter = 0;
+    // The texel of the next step does not depend on this one's value: fetch
+    // it before accumulating the current one so the texture latency overlaps
+    // the step arithmetic.  The fetch after the last step reads a texel the
+    // sum never uses (in range or the zero border).
+    V3 tx = tex_texel<NORM>(tex, px, py, pz);
+    while (t < lim) {
+        if (++iter > cap) { err |= 1u; break; }
+        const float myz = fminf(side.y, side.z);
+        bool mx = side.x <= myz;
+        bool my = side.y <= fminf(side.z, side.x);
+        bool mz = side.z <= fminf(side.x, side.y);
+        float t0 = fminf(side.x, myz);
+        if (COUNT) ++loads;
+        if (mx) { side.x = side.x + t_delta.x; px += sgn.x; }
+        if (my) { side.y = side.y + t_delta.y; py += sgn.y; }
+        if (mz) { side.z = side.z + t_delta.z; pz += sgn.z; }
+        const V3 next = tex_texel<NORM>(tex, px, py, pz);
+        float dt = t0 - t;
+        total = total + tx * dt;
+        t = t0;
+        tx = next;
+    }
+    return total;
+}
+
 // --------------------------------------------------------------- octree ---
 
 // Reference node layout on the device: 10 u32 words per node
@@ -99,6 +165,38 @@ struct RefNodes {
     __device__ __forceinline__ uint32_t child(uint32_t n, uint32_t k) const { return __ldg(w + (uint64_t)n * 10 + k); }
     __device__ __forceinline__ uint32_t color(uint32_t n) const { return __ldg(w + (uint64_t)n * 10 + 8); }
     __device__ __forceinline__ uint32_t depth(uint32_t n) const { return __ldg(w + (uint64_t)n * 10 + 9) & DEPTH_MASK; }
+    __device__ __forceinline__ uint32_t exit_word() const { return 0; }
+};
+
+// Compact layout (svo_layout.cu) for svo-naive, svo-df and esvo: handles are
+// child words; a leaf word carries the leaf's RGB.
+struct CompactNodes {
+    const uint32_t* inner;
+    const uint32_t* depth_of;
+    __device__ __forceinline__ uint32_t root() const { return 0; }
+    __device__ __forceinline__ bool is_leaf(uint32_t r) const { return r >= LEAF_MASK; }
+    __device__ __forceinline__ uint32_t child(uint32_t r, uint32_t k) const { return __ldg(inner + (uint64_t)r * 8 + k); }
+    __device__ __forceinline__ uint32_t color(uint32_t r) const { return r & 0xFFFFFFu; }
+    __device__ __forceinline__ uint32_t depth(uint32_t r) const { return __ldg(depth_of + r) & DEPTH_MASK; }
+    __device__ __forceinline__ uint32_t exit_word() const { return 0; }
+};
+
+// Compact layout for svo-rope: a leaf word carries the index of the leaf's
+// record (colour, six ropes, is_leaf_depth); the children of a leaf are its ropes.
+struct RopeNodes {
+    const uint32_t* inner;
+    const uint32_t* depth_of;
+    const uint32_t* leaves;
+    __device__ __forceinline__ uint32_t root() const { return 0; }
+    __device__ __forceinline__ bool is_leaf(uint32_t r) const { return r >= LEAF_MASK; }
+    __device__ __forceinline__ uint32_t child(uint32_t r, uint32_t k) const {
+        return r >= LEAF_MASK ? __ldg(leaves + (uint64_t)(r & DEPTH_MASK) * 8 + 1 + k) : __ldg(inner + (uint64_t)r * 8 + k);
+    }
+    __device__ __forceinline__ uint32_t color(uint32_t r) const { return __ldg(leaves + (uint64_t)(r & DEPTH_MASK) * 8); }
+    __device__ __forceinline__ uint32_t depth(uint32_t r) const {
+        return (r >= LEAF_MASK ? __ldg(leaves + (uint64_t)(r & DEPTH_MASK) * 8 + 7) : __ldg(depth_of + r)) & DEPTH_MASK;
+    }
+    __device__ __forceinline__ uint32_t exit_word() const { return ROPE_EXIT; }
 };
 
 // resources/svo_naive.comp:8-27 (identical to svo_rope.comp:8-27); reads per
@@ -127,6 +225,72 @@ __device__ __forceinline__ uint32_t find(const Acc& a, V3 pos, V3& base, float& 
     }
 }
 
+// find() resumed from the previous step's path.  find(p) depends only on p:
+// the descent from the root reaches node A at depth j exactly when p lies in
+// A's capture region, per axis [O_A, O_A + 2^-j) with a bound replaced by
+// -inf/+inf where it is the root's (O_A == 0 / O_A + 2^-j == 1), O_A being
+// A's origin, which the root descent computes exactly (dyadic sums).  So the
+// descent can restart at the deepest node of the last path whose region holds
+// p, with the same offsets and extents, and reach the same leaf with the same
+// base and side.  The reference's word reads are still 2 per level + 1.
+constexpr int PATH_CACHE = 32;
+
+struct FindPath {
+    uint32_t node[PATH_CACHE];
+    int depth = -1;  // depth of the last leaf found, -1: none (or too deep to cache)
+    V3 base;         // the last leaf's origin
+};
+
+__device__ __forceinline__ bool in_capture(float p, float o, float size) {
+    return (o == 0.0f || p >= o) && (o + size == 1.0f || p < o + size);
+}
+
+template <bool COUNT, class Acc>
+__device__ __forceinline__ uint32_t find_cached(const Acc& a, FindPath& path, V3 pos, V3& base, float& side,
+                                                uint32_t& loads, uint32_t& err) {
+    int level = 0;
+    float extent = 1.0f;
+    uint32_t index = a.root();
+    V3 offset = vs(0.0f);
+    for (int j = path.depth; j > 0; --j) {
+        const float size = ldexpf(1.0f, -j);
+        const float inv = ldexpf(1.0f, j);
+        const V3 o = v3(floorf(path.base.x * inv) * size, floorf(path.base.y * inv) * size,
+                        floorf(path.base.z * inv) * size);
+        if (in_capture(pos.x, o.x, size) && in_capture(pos.y, o.y, size) && in_capture(pos.z, o.z, size)) {
+            level = j;
+            extent = size;
+            index = path.node[j];
+            offset = o;
+            break;
+        }
+    }
+    for (;; ++level) {
+        if (level < PATH_CACHE) path.node[level] = index;
+        if (a.is_leaf(index)) {
+            base = offset;
+            side = extent;
+            if (COUNT) loads += 2u * (uint32_t)level + 1u;
+            path.depth = level < PATH_CACHE ? level : -1;
+            path.base = offset;
+            return index;
+        }
+        if (level >= FIND_MAX_DEPTH) {
+            err |= 1u;
+            base = offset;
+            side = extent;
+            path.depth = -1;
+            return index;
+        }
+        extent *= 0.5f;
+        V3 oe = offset + vs(extent);
+        bool mx = pos.x >= oe.x, my = pos.y >= oe.y, mz = pos.z >= oe.z;
+        uint32_t child = (mx ? 4u : 0u) | (my ? 2u : 0u) | (mz ? 1u : 0u);
+        offset = offset + v3(mx ? 1.0f : 0.0f, my ? 1.0f : 0.0f, mz ? 1.0f : 0.0f) * vs(extent);
+        index = a.child(index, child);
+    }
+}
+
 // resources/svo_naive.comp:29-71
 template <bool COUNT, class Acc>
 __device__ V3 trace_naive(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& err) {
@@ -142,12 +306,13 @@ __device__ V3 trace_naive(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t&
     V3 total = vs(0.0f);
     float t = t_min + MIN_STEP;
     uint32_t iter = 0;
+    FindPath path;
     while (t < t_max) {
         if (++iter > SVO_MAX_ITER) { err |= 1u; break; }
         V3 p = rd * t + ro;
         V3 offset;
         float side;
-        uint32_t node = find<COUNT>(a, p, offset, side, loads, err);
+        uint32_t node = find_cached<COUNT>(a, path, p, offset, side, loads, err);
         V3 node_min = offset * rrd - bias;
         V3 node_max = (offset + vs(side)) * rrd - bias;
         float u_min = max_elem(vmin(node_min, node_max));
@@ -174,6 +339,8 @@ __device__ V3 trace_df(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& er
     uint32_t child_idx = 0;
     V3 pos = vs(0.0f);
     float side = 0.5f;
+    float s2_cached = -1.0f, s2_inv = 0.0f;
+    bool s2_exact = false;
     V3 total = vs(0.0f);
     uint32_t iter = 0;
     for (;;) {
@@ -212,12 +379,140 @@ __device__ V3 trace_df(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& er
             if (COUNT) ++loads;
             side = ldexpf(1.0f, -(int)(d > 1000u ? 1000u : d)) * 0.5f;
         }
-        float s2 = side * 2.0f;
-        pos = pos - v3(gl_mod(pos.x, s2), gl_mod(pos.y, s2), gl_mod(pos.z, s2));
+        const float s2 = side * 2.0f;
+        if (s2 != s2_cached) {  // side changes only on a push or a pop
+            s2_cached = s2;
+            s2_exact = pow2_with_normal_reciprocal(s2);
+            s2_inv = __frcp_rn(s2);
+        }
+        pos = pos - v3(gl_mod_pow2(pos.x, s2, s2_inv, s2_exact), gl_mod_pow2(pos.y, s2, s2_inv, s2_exact),
+                       gl_mod_pow2(pos.z, s2, s2_inv, s2_exact));
         ++child_idx;
         if (child_idx & 4u) pos.x = pos.x + side;
         if (child_idx & 2u) pos.y = pos.y + side;
         if (child_idx & 1u) pos.z = pos.z + side;
+    }
+    return total;
+}
+
+// resources/svo_df.comp:6-67 for octrees whose depth fields match the tree
+// (checked on upload; every octree the reference's builder writes does).
+// The reference tests the 8 child boxes of a node one loop iteration at a
+// time.  Here the 8 boxes of a node are tested together: with node origin O
+// and child size s, the reference's box_min/box_max floats of child k are, per
+// axis, two of the three plane distances O*rrd-bias, (O+s)*rrd-bias and
+// ((O+s)+s)*rrd-bias (positions are dyadic, so these sums are exactly the
+// reference's `pos` values), giving a hit mask; then the hit children are
+// visited in index order.  Accumulation order and every accumulated value are
+// the reference's, so the result is bit-identical; so is the word-read count.
+// Plane distances of the 8 child boxes of one node: per axis the lower and
+// upper bound of the low child (l0, h0) and of the high child (l1, h1).
+struct ChildSlabs {
+    float xl0, xl1, xh0, xh1, yl0, yl1, yh0, yh1, zl0, zl1, zh0, zh1;
+};
+
+__device__ __forceinline__ ChildSlabs child_slabs(V3 origin, float s, V3 rrd, V3 bias) {
+    const float px1 = origin.x + s, py1 = origin.y + s, pz1 = origin.z + s;
+    const float x0 = origin.x * rrd.x - bias.x, x1 = px1 * rrd.x - bias.x, x2 = (px1 + s) * rrd.x - bias.x;
+    const float y0 = origin.y * rrd.y - bias.y, y1 = py1 * rrd.y - bias.y, y2 = (py1 + s) * rrd.y - bias.y;
+    const float z0 = origin.z * rrd.z - bias.z, z1 = pz1 * rrd.z - bias.z, z2 = (pz1 + s) * rrd.z - bias.z;
+    return ChildSlabs{fminf(x0, x1), fminf(x1, x2), fmaxf(x0, x1), fmaxf(x1, x2),
+                      fminf(y0, y1), fminf(y1, y2), fmaxf(y0, y1), fmaxf(y1, y2),
+                      fminf(z0, z1), fminf(z1, z2), fmaxf(z0, z1), fmaxf(z1, z2)};
+}
+
+// t_min / t_max of child k, as the reference computes them for that box
+__device__ __forceinline__ void child_span(const ChildSlabs& c, uint32_t k, float& t0, float& t1) {
+    const bool bx = k & 4u, by = k & 2u, bz = k & 1u;
+    t0 = fmaxf(bx ? c.xl1 : c.xl0, fmaxf(by ? c.yl1 : c.yl0, bz ? c.zl1 : c.zl0));
+    t1 = fminf(bx ? c.xh1 : c.xh0, fminf(by ? c.yh1 : c.yh0, bz ? c.zh1 : c.zh0));
+}
+
+__device__ __forceinline__ uint32_t hit_mask(const ChildSlabs& c) {
+    uint32_t m = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < 8; ++k) {
+        float t0, t1;
+        child_span(c, k, t0, t1);
+        if (t0 < t1 && t1 > 0.0f) m |= 1u << k;
+    }
+    return m;
+}
+
+// resources/svo_df.comp:6-67 for octrees whose depth fields match the tree
+// (checked on upload; every octree the reference's builder writes does).
+// The reference tests the 8 child boxes of a node one loop iteration at a
+// time.  Here they are tested together: with node origin O and child size s,
+// child k's box_min/box_max floats are, per axis, two of the plane distances
+// O*rrd-bias, (O+s)*rrd-bias and ((O+s)+s)*rrd-bias (positions are dyadic, so
+// these sums are exactly the reference's `pos` values), which gives a hit
+// mask; the hit children are then visited in index order.  Pushes and pops
+// happen exactly where the reference's do, the accumulation order and every
+// accumulated value are the reference's, so the result is bit-identical, and
+// so is the count of words the reference reads.
+template <bool COUNT, class Acc>
+__device__ V3 trace_df_masked(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& err) {
+    const V3 rrd = vs(1.0f) / rd;
+    const V3 bias = rrd * ro;
+    uint32_t node_stack[STACK_DEPTH];
+    uint32_t state_stack[STACK_DEPTH];  // remaining hit mask | depth << 8
+    int sp = 0;
+    uint32_t node = a.root();
+    uint32_t depth = 0;
+    V3 origin = vs(0.0f);
+    float side = 0.5f;  // child box size of `node`
+    V3 total = vs(0.0f);
+    ChildSlabs slabs = child_slabs(origin, side, rrd, bias);
+    uint32_t mask = hit_mask(slabs);
+    if (COUNT) loads += 8;  // the reference reads children[0..7] of every node it visits
+    uint32_t iter = 0;
+    for (;;) {
+        if (++iter > SVO_MAX_ITER) { err |= 1u; break; }
+        if (mask == 0) {
+            // node finished: the reference pops, reading the parent's depth
+            --sp;
+            if (sp < 0) break;
+            node = node_stack[sp];
+            const uint32_t st = state_stack[sp];
+            mask = st & 0xFFu;
+            depth = st >> 8;
+            if (COUNT) ++loads;
+            side = ldexpf(1.0f, -(int)(depth > 1000u ? 1000u : depth)) * 0.5f;
+            const float s2 = side * 2.0f;
+            const float inv = __frcp_rn(s2);
+            const bool ex = pow2_with_normal_reciprocal(s2);
+            origin = origin - v3(gl_mod_pow2(origin.x, s2, inv, ex), gl_mod_pow2(origin.y, s2, inv, ex),
+                                 gl_mod_pow2(origin.z, s2, inv, ex));
+            slabs = child_slabs(origin, side, rrd, bias);
+            continue;
+        }
+        const uint32_t k = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const uint32_t child = a.child(node, k);
+        if (COUNT) ++loads;  // is_leaf_depth of the hit child
+        float t0, t1;
+        child_span(slabs, k, t0, t1);
+        if (a.is_leaf(child)) {
+            const V3 color = unpack_rgb(a.color(child));
+            if (COUNT) ++loads;
+            total = total + color * (t1 - fmaxf(t0, 0.0f));
+            continue;
+        }
+        // descend into child k; the reference pushes unless k == 7
+        if (k != 7) {
+            if (sp >= STACK_DEPTH) { err |= 2u; break; }
+            node_stack[sp] = node;
+            state_stack[sp] = mask | (depth << 8);
+            ++sp;
+        }
+        origin = v3(origin.x + ((k & 4u) ? side : 0.0f), origin.y + ((k & 2u) ? side : 0.0f),
+                    origin.z + ((k & 1u) ? side : 0.0f));
+        node = child;
+        ++depth;
+        side *= 0.5f;
+        slabs = child_slabs(origin, side, rrd, bias);
+        mask = hit_mask(slabs);
+        if (COUNT) loads += 8;
     }
     return total;
 }
@@ -398,7 +693,7 @@ __device__ V3 trace_rope(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& 
     if (COUNT) loads += 2;
     offset = offset + (mask * sgn) * side;
     uint32_t iter = 0;
-    while (node != 0) {
+    while (node != a.exit_word()) {
         if (++iter > SVO_MAX_ITER) { err |= 1u; break; }
         pos = ro + rd * u_max;
         node = find_relative<COUNT>(a, node, offset, pos, offset, side, loads, err);
@@ -468,6 +763,21 @@ __global__ void __launch_bounds__(BLOCK_THREADS) dda_kernel(Frame f, GridVol g, 
     write_outputs(f, o, ix, iy, color, loads, err);
 }
 
+template <bool COUNT, bool NORM>
+__global__ void __launch_bounds__(BLOCK_THREADS) dda_tex_kernel(Frame f, cudaTextureObject_t tex, uint32_t dx,
+                                                               uint32_t dy, uint32_t dz, Outputs o) {
+    uint32_t ix, iy;
+    if (!pixel_of_thread(f, ix, iy)) return;
+    uint32_t m = max(dx, max(dy, dz));
+    float side = (float)m;
+    V3 ro = f.translation * side;
+    V3 rd = primary_ray(f, ix, iy);
+    float ec = __fdiv_rn(voxel_emission_coeff(f, rd), side);
+    uint32_t loads = 0, err = 0;
+    V3 color = trace_dda_tex<COUNT, NORM>(tex, dx, dy, dz, ro, rd, loads, err) * ec;
+    write_outputs(f, o, ix, iy, color, loads, err);
+}
+
 template <int TRAV, bool COUNT, class Acc>
 __global__ void __launch_bounds__(BLOCK_THREADS) svo_kernel(Frame f, Acc a, Outputs o) {
     uint32_t ix, iy;
@@ -485,6 +795,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS) svo_kernel(Frame f, Acc a, Outp
         total = trace_naive<COUNT>(a, f.translation, rd, loads, err);
     } else if (TRAV == XN_TRAV_SVO_DF) {
         total = trace_df<COUNT>(a, f.translation, rd, loads, err);
+    } else if (TRAV == XN_TRAV_SVO_DF_MASKED) {
+        total = trace_df_masked<COUNT>(a, f.translation, rd, loads, err);
     } else {
         total = trace_rope<COUNT>(a, f.translation, rd, loads, err);
     }
@@ -492,16 +804,22 @@ __global__ void __launch_bounds__(BLOCK_THREADS) svo_kernel(Frame f, Acc a, Outp
     write_outputs(f, o, ix, iy, color, loads, err);
 }
 
-template <int TRAV, bool COUNT>
-static void launch_svo(const Frame& f, const RefNodes& a, const Outputs& o, dim3 grid, cudaStream_t s) {
-    svo_kernel<TRAV, COUNT, RefNodes><<<grid, BLOCK_THREADS, 0, s>>>(f, a, o);
+template <int TRAV, class Acc>
+static void launch_svo_any(bool count, const Frame& f, const Acc& a, const Outputs& o, dim3 grid, cudaStream_t s) {
+    if (count) svo_kernel<TRAV, true, Acc><<<grid, BLOCK_THREADS, 0, s>>>(f, a, o);
+    else svo_kernel<TRAV, false, Acc><<<grid, BLOCK_THREADS, 0, s>>>(f, a, o);
 }
 
-template <int TRAV>
-static void launch_svo_any(bool count, const Frame& f, const RefNodes& a, const Outputs& o, dim3 grid,
-                           cudaStream_t s) {
-    if (count) launch_svo<TRAV, true>(f, a, o, grid, s);
-    else launch_svo<TRAV, false>(f, a, o, grid, s);
+template <class Acc>
+static void launch_traversal(int traversal, bool count, const Frame& f, const Acc& a, const Outputs& o, dim3 grid,
+                             cudaStream_t s) {
+    switch (traversal) {
+    case XN_TRAV_SVO_NAIVE: launch_svo_any<XN_TRAV_SVO_NAIVE>(count, f, a, o, grid, s); break;
+    case XN_TRAV_ESVO: launch_svo_any<XN_TRAV_ESVO>(count, f, a, o, grid, s); break;
+    case XN_TRAV_SVO_DF: launch_svo_any<XN_TRAV_SVO_DF>(count, f, a, o, grid, s); break;
+    case XN_TRAV_SVO_DF_MASKED: launch_svo_any<XN_TRAV_SVO_DF_MASKED>(count, f, a, o, grid, s); break;
+    default: launch_svo_any<XN_TRAV_SVO_ROPE>(count, f, a, o, grid, s); break;
+    }
 }
 
 cudaError_t launch_render(const RenderLaunch& L, cudaStream_t stream) {
@@ -523,21 +841,227 @@ cudaError_t launch_render(const RenderLaunch& L, cudaStream_t stream) {
     Outputs o{static_cast<uint32_t*>(L.d_rgba), L.d_emission, L.d_loads, L.d_err_word};
     dim3 grid((L.out_w + TILE_W - 1) / TILE_W, (L.out_h + TILE_H - 1) / TILE_H);
     const bool count = L.d_loads != nullptr;
-    if (L.traversal == XN_TRAV_DDA) {
+    if (L.traversal == XN_TRAV_DDA && L.tex) {
+        const cudaTextureObject_t t = L.tex;
+        if (L.tex_normalized) {
+            if (count) dda_tex_kernel<true, true><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, L.dim[0], L.dim[1], L.dim[2], o);
+            else dda_tex_kernel<false, true><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, L.dim[0], L.dim[1], L.dim[2], o);
+        } else {
+            if (count) dda_tex_kernel<true, false><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, L.dim[0], L.dim[1], L.dim[2], o);
+            else dda_tex_kernel<false, false><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, L.dim[0], L.dim[1], L.dim[2], o);
+        }
+    } else if (L.traversal == XN_TRAV_DDA) {
         GridVol g{static_cast<const uchar4*>(L.grid), L.dim[0], L.dim[1], L.dim[2], (uint64_t)L.dim[0],
                   (uint64_t)L.dim[0] * L.dim[1]};
         if (count) dda_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, g, o);
         else dda_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, g, o);
+    } else if (L.layout == XN_LAYOUT_REFERENCE) {
+        launch_traversal(L.traversal, count, f, RefNodes{static_cast<const uint32_t*>(L.nodes)}, o, grid, stream);
+    } else if (L.traversal == XN_TRAV_SVO_ROPE) {
+        launch_traversal(L.traversal, count, f, RopeNodes{L.rinner, L.inner_depth, L.leaves}, o, grid, stream);
     } else {
-        RefNodes a{static_cast<const uint32_t*>(L.nodes)};
-        switch (L.traversal) {
-        case XN_TRAV_SVO_NAIVE: launch_svo_any<XN_TRAV_SVO_NAIVE>(count, f, a, o, grid, stream); break;
-        case XN_TRAV_ESVO: launch_svo_any<XN_TRAV_ESVO>(count, f, a, o, grid, stream); break;
-        case XN_TRAV_SVO_DF: launch_svo_any<XN_TRAV_SVO_DF>(count, f, a, o, grid, stream); break;
-        default: launch_svo_any<XN_TRAV_SVO_ROPE>(count, f, a, o, grid, stream); break;
-        }
+        const int trav = L.traversal == XN_TRAV_SVO_DF && L.depth_consistent ? XN_TRAV_SVO_DF_MASKED : L.traversal;
+        launch_traversal(trav, count, f, CompactNodes{L.inner, L.inner_depth}, o, grid, stream);
     }
     return cudaGetLastError();
+}
+
+}  // namespace xn
+
+// ------------------------------------------------------- persistent batch ---
+//
+// One launch renders many jobs (cameras x volumes x traversals x
+// resolutions).  The jobs' warp tiles (tile_w x 32/tile_w pixels) form one
+// sequence; resident warps take `chunk` tiles at a time from a global counter
+// (one atomic per warp per chunk) until the sequence is exhausted, so uneven
+// jobs balance across the SMs and small frames fill the GPU together.
+
+namespace xn {
+
+BatchJob make_batch_job(const RenderLaunch& L) {
+    BatchJob j{};
+    for (int i = 0; i < 3; ++i) {
+        j.forward[i] = L.forward[i];
+        j.up[i] = L.up[i];
+        j.translation[i] = L.translation[i];
+        j.voxel_ratio[i] = L.voxel_ratio[i];
+        j.dim[i] = L.dim[i];
+    }
+    j.aspect = L.aspect;
+    j.emission_coeff = L.emission_coeff;
+    j.out_x = L.out_x;
+    j.out_y = L.out_y;
+    j.out_w = L.out_w;
+    j.out_h = L.out_h;
+    j.disp_x = L.disp_x;
+    j.disp_y = L.disp_y;
+    j.disp_w = L.disp_w;
+    j.disp_h = L.disp_h;
+    j.traversal = L.traversal;
+    j.tex = L.tex;
+    j.tex_normalized = L.tex_normalized;
+    j.layout = L.traversal == XN_TRAV_DDA ? (L.tex ? 1 : 0) : L.layout;
+    j.grid = L.grid;
+    j.nodes = L.nodes;
+    j.inner = L.inner;
+    j.rinner = L.rinner;
+    j.inner_depth = L.inner_depth;
+    j.leaves = L.leaves;
+    j.rgba = L.d_rgba;
+    j.depth_consistent = L.depth_consistent;
+    return j;
+}
+
+__device__ __forceinline__ Frame frame_of(const BatchJob& J) {
+    Frame f;
+    f.forward = v3(J.forward[0], J.forward[1], J.forward[2]);
+    f.up = v3(J.up[0], J.up[1], J.up[2]);
+    f.translation = v3(J.translation[0], J.translation[1], J.translation[2]);
+    f.voxel_ratio = v3(J.voxel_ratio[0], J.voxel_ratio[1], J.voxel_ratio[2]);
+    f.aspect = J.aspect;
+    f.emission_coeff = J.emission_coeff;
+    f.out_x = J.out_x;
+    f.out_y = J.out_y;
+    f.out_w = J.out_w;
+    f.out_h = J.out_h;
+    f.disp_x = J.disp_x;
+    f.disp_y = J.disp_y;
+    f.disp_w = J.disp_w;
+    f.disp_h = J.disp_h;
+    return f;
+}
+
+template <int TRAV, class Acc>
+__device__ __forceinline__ V3 trace_svo_job(const Acc& a, const Frame& f, V3 rd, uint32_t& loads, uint32_t& err) {
+    if (TRAV == XN_TRAV_ESVO) {
+        V3 ro = f.translation + vs(1.0f);
+        float t0 = aabb_entry(vs(1.0f), vs(2.0f), ro, rd);
+        ro = ro + rd * fmaxf(t0, 0.0f);
+        return trace_esvo<false>(a, ro, rd, loads, err);
+    } else if (TRAV == XN_TRAV_SVO_NAIVE) {
+        return trace_naive<false>(a, f.translation, rd, loads, err);
+    } else if (TRAV == XN_TRAV_SVO_DF) {
+        return trace_df<false>(a, f.translation, rd, loads, err);
+    } else if (TRAV == XN_TRAV_SVO_DF_MASKED) {
+        return trace_df_masked<false>(a, f.translation, rd, loads, err);
+    }
+    return trace_rope<false>(a, f.translation, rd, loads, err);
+}
+
+// One pixel of one job: the same arithmetic as the single-frame kernels.
+__device__ __noinline__ uint32_t render_job_pixel(const BatchJob& J, uint32_t ix, uint32_t iy, uint32_t& err) {
+    const Frame f = frame_of(J);
+    const V3 rd = primary_ray(f, ix, iy);
+    uint32_t loads = 0;
+    V3 color;
+    if (J.traversal == XN_TRAV_DDA) {
+        const uint32_t m = max(J.dim[0], max(J.dim[1], J.dim[2]));
+        const float side = (float)m;
+        const V3 ro = f.translation * side;
+        const float ec = __fdiv_rn(voxel_emission_coeff(f, rd), side);
+        V3 total;
+        if (J.layout == 1) {
+            total = J.tex_normalized
+                        ? trace_dda_tex<false, true>(J.tex, J.dim[0], J.dim[1], J.dim[2], ro, rd, loads, err)
+                        : trace_dda_tex<false, false>(J.tex, J.dim[0], J.dim[1], J.dim[2], ro, rd, loads, err);
+        } else {
+            GridVol g{static_cast<const uchar4*>(J.grid), J.dim[0], J.dim[1], J.dim[2], (uint64_t)J.dim[0],
+                      (uint64_t)J.dim[0] * J.dim[1]};
+            total = trace_dda<false>(g, ro, rd, loads, err);
+        }
+        color = total * ec;
+    } else {
+        V3 total;
+        if (J.layout == XN_LAYOUT_REFERENCE) {
+            RefNodes a{static_cast<const uint32_t*>(J.nodes)};
+            switch (J.traversal) {
+            case XN_TRAV_SVO_NAIVE: total = trace_svo_job<XN_TRAV_SVO_NAIVE>(a, f, rd, loads, err); break;
+            case XN_TRAV_ESVO: total = trace_svo_job<XN_TRAV_ESVO>(a, f, rd, loads, err); break;
+            case XN_TRAV_SVO_DF: total = trace_svo_job<XN_TRAV_SVO_DF>(a, f, rd, loads, err); break;
+            default: total = trace_svo_job<XN_TRAV_SVO_ROPE>(a, f, rd, loads, err); break;
+            }
+        } else if (J.traversal == XN_TRAV_SVO_ROPE) {
+            total = trace_svo_job<XN_TRAV_SVO_ROPE>(RopeNodes{J.rinner, J.inner_depth, J.leaves}, f, rd, loads, err);
+        } else {
+            CompactNodes a{J.inner, J.inner_depth};
+            switch (J.traversal) {
+            case XN_TRAV_SVO_NAIVE: total = trace_svo_job<XN_TRAV_SVO_NAIVE>(a, f, rd, loads, err); break;
+            case XN_TRAV_ESVO: total = trace_svo_job<XN_TRAV_ESVO>(a, f, rd, loads, err); break;
+            default:
+                total = J.depth_consistent ? trace_svo_job<XN_TRAV_SVO_DF_MASKED>(a, f, rd, loads, err)
+                                           : trace_svo_job<XN_TRAV_SVO_DF>(a, f, rd, loads, err);
+                break;
+            }
+        }
+        color = total * voxel_emission_coeff(f, rd);
+    }
+    return pack_rgba(color);
+}
+
+template <int TW>
+__global__ void __launch_bounds__(1024) batch_kernel(const BatchHeader* hdr, const BatchJob* jobs,
+                                                     unsigned long long* queue, uint32_t chunk, uint32_t* err_word) {
+    constexpr int TH = 32 / TW;
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned long long total = hdr->total_tiles;
+    const uint32_t n = hdr->n_jobs;
+    uint32_t err = 0;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(queue, (unsigned long long)chunk);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= total) break;
+        const unsigned long long end = base + chunk < total ? base + chunk : total;
+        for (unsigned long long t = base; t < end; ++t) {
+            uint32_t lo = 0, hi = n;  // last job whose first tile is <= t
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (jobs[mid].tile_begin <= t) lo = mid;
+                else hi = mid;
+            }
+            const BatchJob& J = jobs[lo];
+            const unsigned long long local = t - J.tile_begin;
+            const uint32_t ty = (uint32_t)(local / J.tiles_x);
+            const uint32_t tx = (uint32_t)(local - (unsigned long long)ty * J.tiles_x);
+            const uint32_t ix = tx * TW + lane % TW, iy = ty * TH + lane / TW;
+            if (ix < J.out_w && iy < J.out_h) {
+                const uint32_t px = render_job_pixel(J, ix, iy, err);
+                static_cast<uint32_t*>(J.rgba)[(uint64_t)iy * J.out_w + ix] = px;
+            }
+        }
+    }
+    if (err) atomicOr(err_word, err);
+}
+
+template <int TW>
+static cudaError_t launch_batch_tw(const void* table, unsigned long long* q, uint32_t* err, uint32_t threads,
+                                   uint32_t blocks, uint32_t chunk, cudaStream_t s) {
+    const BatchHeader* hdr = static_cast<const BatchHeader*>(table);
+    const BatchJob* jobs = reinterpret_cast<const BatchJob*>(hdr + 1);
+    batch_kernel<TW><<<blocks, threads, 0, s>>>(hdr, jobs, q, chunk, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch(const void* table, unsigned long long* q, uint32_t* err, uint32_t tile_w,
+                         uint32_t threads, uint32_t blocks, uint32_t chunk, cudaStream_t s) {
+    switch (tile_w) {
+    case 4: return launch_batch_tw<4>(table, q, err, threads, blocks, chunk, s);
+    case 16: return launch_batch_tw<16>(table, q, err, threads, blocks, chunk, s);
+    case 32: return launch_batch_tw<32>(table, q, err, threads, blocks, chunk, s);
+    default: return launch_batch_tw<8>(table, q, err, threads, blocks, chunk, s);
+    }
+}
+
+int batch_kernel_blocks_per_sm(uint32_t tile_w, uint32_t threads) {
+    int n = 0;
+    cudaError_t e;
+    switch (tile_w) {
+    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<4>, (int)threads, 0); break;
+    case 16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<16>, (int)threads, 0); break;
+    case 32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<32>, (int)threads, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<8>, (int)threads, 0); break;
+    }
+    return e == cudaSuccess ? n : 0;
 }
 
 }  // namespace xn

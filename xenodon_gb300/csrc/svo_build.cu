@@ -29,13 +29,17 @@
 #include <cstdlib>
 #include <cstring>
 #include <algorithm>
+#include <new>
 #include <vector>
 
 #include "../../include/xenodon.h"
 #include "xn_ctx.h"
+#include "xn_scan.cuh"
 
 namespace xn {
 namespace {
+
+using namespace scan;
 
 constexpr uint32_t LEAF = 0x80000000u;
 constexpr uint64_t NONE = ~0ull;
@@ -621,71 +625,6 @@ __global__ void dag_write_kernel(DagLevel a, const unsigned int* ins, uint64_t U
     if ((threadIdx.x & 31) == 0 && ul) atomicAdd(unique_leaves, ul);
 }
 
-// ------------------------------------------------------------------- scan ---
-
-constexpr int SCAN_T = 256;
-constexpr int SCAN_ITEMS = 16;
-constexpr uint64_t SCAN_CHUNK = (uint64_t)SCAN_T * SCAN_ITEMS;
-
-__device__ __forceinline__ unsigned block_exclusive_scan(unsigned v) {
-    __shared__ unsigned warp_sums[SCAN_T / 32];
-    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned incl = v;
-    for (int o = 1; o < 32; o <<= 1) {
-        unsigned t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= (unsigned)o) incl += t;
-    }
-    if (lane == 31) warp_sums[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-        unsigned w = lane < SCAN_T / 32 ? warp_sums[lane] : 0u;
-        unsigned wi = w;
-        for (int o = 1; o < 32; o <<= 1) {
-            unsigned t = __shfl_up_sync(0xFFFFFFFFu, wi, o);
-            if (lane >= (unsigned)o) wi += t;
-        }
-        if (lane < SCAN_T / 32) warp_sums[lane] = wi - w;
-    }
-    __syncthreads();
-    return warp_sums[warp] + incl - v;
-}
-
-template <class In>
-__global__ void scan_reduce_kernel(const In* in, uint64_t n, unsigned* block_sums) {
-    const uint64_t base = (uint64_t)blockIdx.x * SCAN_CHUNK + (uint64_t)threadIdx.x * SCAN_ITEMS;
-    unsigned s = 0;
-#pragma unroll
-    for (int j = 0; j < SCAN_ITEMS; ++j)
-        if (base + j < n) s += (unsigned)in[base + j];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, o);
-    __shared__ unsigned ws[SCAN_T / 32];
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned t = 0;
-        for (int w = 0; w < SCAN_T / 32; ++w) t += ws[w];
-        block_sums[blockIdx.x] = t;
-    }
-}
-
-template <class In>
-__global__ void scan_apply_kernel(const In* in, uint64_t n, const unsigned* block_offsets, unsigned* out) {
-    const uint64_t base = (uint64_t)blockIdx.x * SCAN_CHUNK + (uint64_t)threadIdx.x * SCAN_ITEMS;
-    unsigned v[SCAN_ITEMS];
-    unsigned s = 0;
-#pragma unroll
-    for (int j = 0; j < SCAN_ITEMS; ++j) {
-        v[j] = base + j < n ? (unsigned)in[base + j] : 0u;
-        s += v[j];
-    }
-    unsigned run = block_exclusive_scan(s) + (block_offsets ? block_offsets[blockIdx.x] : 0u);
-#pragma unroll
-    for (int j = 0; j < SCAN_ITEMS; ++j) {
-        if (base + j < n) out[base + j] = run;
-        run += v[j];
-    }
-}
-
 uint64_t ceil_pow2(uint64_t x) {
     --x;
     x |= x >> 1;
@@ -1092,6 +1031,53 @@ XN_API int xn_build_svo(xn_ctx* h, const uint8_t* rgba, uint32_t dx, uint32_t dy
         return cuda_fail(e, "xn_build_svo: download");
     }
     *nodes_out = host;
+    return XN_OK;
+}
+
+XN_API int xn_build_svo_volume(xn_ctx* h, const void* d_rgba, uint32_t dx, uint32_t dy, uint32_t dz, int type,
+                               int heuristic, double threshold, xn_volume** out, xn_build_stats* stats) {
+    if (!h || !d_rgba || !out || !stats) return fail(XN_ERR_ARG, "xn_build_svo_volume: NULL argument");
+    *out = nullptr;
+    if (!dx || !dy || !dz) return fail(XN_ERR_ARG, "xn_build_svo_volume: empty grid %ux%ux%u", dx, dy, dz);
+    if (type < XN_SVO_SPARSE || type > XN_SVO_ROPE_TREE)
+        return fail(XN_ERR_ARG, "xn_build_svo_volume: invalid type %d", type);
+    if (heuristic == XN_HEUR_CHANNEL_DIFF) {
+        if (!(threshold >= 0.0 && threshold <= 255.0) || threshold != (double)(int)threshold)
+            return fail(XN_ERR_ARG, "xn_build_svo_volume: --chan-diff must be an integer in 0..255");
+    } else if (heuristic == XN_HEUR_STD_DEV) {
+        if (!(threshold >= 0.0)) return fail(XN_ERR_ARG, "xn_build_svo_volume: --std-dev must be >= 0");
+    } else {
+        return fail(XN_ERR_ARG, "xn_build_svo_volume: invalid heuristic %d", heuristic);
+    }
+    Ctx* c = reinterpret_cast<Ctx*>(h);
+    std::lock_guard<std::mutex> lk(c->mu);
+    int r = c->activate();
+    if (r) return r;
+    uint32_t* d_nodes = nullptr;
+    uint64_t nbytes = 0;
+    r = build_svo_device(c, static_cast<const uint32_t*>(d_rgba), dx, dy, dz, type, heuristic, threshold, &d_nodes,
+                         &nbytes, stats);
+    if (r) return r;
+    Volume* v = new (std::nothrow) Volume();
+    if (!v) {
+        c->device_free(d_nodes, nbytes);
+        return fail(XN_ERR_NOMEM, "xn_build_svo_volume: out of host memory");
+    }
+    v->ctx = c;
+    v->kind = XN_VOLUME_SVO;
+    v->side = stats->side;
+    v->n_nodes = stats->n_nodes;
+    const uint64_t sd = stats->side > 0xFFFFFFFFull ? 0xFFFFFFFFull : stats->side;
+    v->dim[0] = v->dim[1] = v->dim[2] = (uint32_t)sd;
+    v->data = d_nodes;
+    v->bytes = nbytes;
+    v->has_ropes = type == XN_SVO_ROPE_TREE;
+    if ((r = build_svo_layout(c, v))) {
+        c->device_free(v->data, v->bytes);
+        delete v;
+        return r;
+    }
+    *out = reinterpret_cast<xn_volume*>(v);
     return XN_OK;
 }
 

@@ -7,6 +7,8 @@
 
 #include <cuda_runtime.h>
 
+#include "../../include/xenodon.h"
+
 namespace xn {
 
 struct DeviceBuffer {
@@ -24,7 +26,18 @@ struct Ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     uint32_t* d_err = nullptr;  // ray error bits
     DeviceBuffer out_rgba, out_emission;
+    int tex_norm_exact = -1;  // texture UNORM8 conversion equals byte/255 (-1: not checked yet)
+    // batches (batch.cu)
+    int sms = 0;
+    void* batch_host = nullptr;  // pinned job table
+    uint64_t batch_host_bytes = 0;
+    DeviceBuffer batch_table, batch_queue;
+    cudaEvent_t batch_copied = nullptr;
+    xn_batch_config tuned[32] = {};
+    int tuned_valid[32] = {};
     std::mutex mu;
+
+    int sm_count();
 
     int activate();
     int device_alloc(void** p, uint64_t bytes, const char* what);
@@ -42,7 +55,32 @@ struct Volume {
     int has_ropes = 0;
     void* data = nullptr;  // grid texels or reference node words
     uint64_t bytes = 0;
+    // grid texture form (xn_volume_upload_grid)
+    cudaArray_t array = nullptr;
+    cudaTextureObject_t tex = 0;
+    int tex_normalized = 0;
+    uint64_t array_bytes = 0;
+    // octree device layout (svo_layout.cu)
+    int layout = 0;
+    uint64_t n_inner = 0, n_leaves = 0;
+    uint32_t* inner = nullptr;
+    uint32_t* rinner = nullptr;
+    uint32_t* inner_depth = nullptr;
+    uint32_t* leaves = nullptr;
+    int depth_consistent = 0;  // internal nodes' depth fields match the tree (svo_layout.cu)
+
+    uint64_t layout_bytes() const { return n_inner * 68 + n_leaves * 32; }
+    void release_layout() {
+        if (!ctx) return;
+        ctx->device_free(inner, n_inner * 32);
+        ctx->device_free(rinner, n_inner * 32);
+        ctx->device_free(inner_depth, n_inner * 4);
+        ctx->device_free(leaves, n_leaves * 32);
+        inner = rinner = inner_depth = leaves = nullptr;
+    }
 };
+
+int build_svo_layout(Ctx* c, Volume* v);
 
 int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
 int cuda_fail(cudaError_t e, const char* what);

@@ -41,6 +41,20 @@ __device__ __forceinline__ V3 normalize3(V3 v) {
 __device__ __forceinline__ float gl_sign(float x) { return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f); }
 // GLSL mod: x - y*floor(x/y)
 __device__ __forceinline__ float gl_mod(float x, float y) { return x - y * floorf(__fdiv_rn(x, y)); }
+// GLSL mod(x, y) for y a power of two: x/y is then exactly x * (1/y) (both
+// the reciprocal and the product are exact while 1/y is a normal float), so
+// the IEEE division of gl_mod is replaced by a multiply; any other y falls
+// back to the division.  `inv` is __frcp_rn(y), computed when y changes.
+__device__ __forceinline__ float gl_mod_pow2(float x, float y, float inv, bool exact) {
+    return x - y * floorf(exact ? x * inv : __fdiv_rn(x, y));
+}
+// Whether y is a power of two whose reciprocal is a normal float.
+__device__ __forceinline__ bool pow2_with_normal_reciprocal(float y) {
+    const uint32_t b = __float_as_uint(y);
+    const uint32_t e = (b >> 23) & 0xFFu;
+    return (b & 0x807FFFFFu) == 0 && e >= 2 && e <= 252;
+}
+
 // float -> int truncation, clamped like the oracle (out-of-range values are
 // never used by the shaders).
 __device__ __forceinline__ int f2i(float x) {

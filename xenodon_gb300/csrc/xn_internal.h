@@ -6,12 +6,18 @@
 
 namespace xn {
 
+// device octree layouts (see svo_layout.cu)
+enum { XN_LAYOUT_REFERENCE = 0, XN_LAYOUT_COMPACT = 1 };
+// rope word meaning "no neighbour" in the compact layout (the reference's rope to node 0)
+constexpr uint32_t ROPE_EXIT = 0xFFFFFFFFu;
+
 enum {
     XN_TRAV_DDA = 0,
     XN_TRAV_SVO_NAIVE = 1,
     XN_TRAV_ESVO = 2,
     XN_TRAV_SVO_DF = 3,
-    XN_TRAV_SVO_ROPE = 4
+    XN_TRAV_SVO_ROPE = 4,
+    XN_TRAV_SVO_DF_MASKED = 5  // svo-df on an octree with consistent depth fields (render.cu)
 };
 
 // Everything one traversal launch needs; built by the C-ABI layer from an
@@ -28,9 +34,17 @@ struct RenderLaunch {
     int32_t disp_x, disp_y;
     uint32_t disp_w, disp_h;
     // volume
-    const void* grid;   // uchar4 texels, x fastest (DDA)
+    const void* grid;   // uchar4 texels, x fastest (DDA, linear form)
+    unsigned long long tex;  // cudaTextureObject_t of the texture form, or 0
+    int tex_normalized;      // the texture returns byte/255 itself
     uint32_t dim[3];
-    const void* nodes;  // reference node words (octree traversals)
+    const void* nodes;  // reference node words (octree traversals, reference layout)
+    int layout;
+    const uint32_t* inner;        // compact layout (svo_layout.cu)
+    const uint32_t* rinner;
+    const uint32_t* inner_depth;
+    const uint32_t* leaves;
+    int depth_consistent;         // every internal node's depth field = its depth in the tree
     // outputs (device pointers)
     void* d_rgba;
     float* d_emission;
@@ -39,5 +53,44 @@ struct RenderLaunch {
 };
 
 cudaError_t launch_render(const RenderLaunch& launch, cudaStream_t stream);
+
+// One job of a persistent batch launch (device copy of a RenderLaunch plus its
+// place in the batch's tile sequence).
+struct alignas(16) BatchJob {
+    float forward[3], up[3], translation[3], voxel_ratio[3];
+    float aspect, emission_coeff;
+    int32_t out_x, out_y;
+    uint32_t out_w, out_h;
+    int32_t disp_x, disp_y;
+    uint32_t disp_w, disp_h;
+    int32_t traversal, layout;  // layout: grids 0 linear / 1 texture; octrees XN_LAYOUT_*
+    uint32_t dim[3];
+    int32_t tex_normalized;
+    int32_t depth_consistent;
+    int32_t pad0;
+    unsigned long long tex;
+    const void* grid;
+    const void* nodes;
+    const uint32_t* inner;
+    const uint32_t* rinner;
+    const uint32_t* inner_depth;
+    const uint32_t* leaves;
+    void* rgba;
+    uint32_t tiles_x, tiles_y;
+    unsigned long long tile_begin;  // first tile of this job in the batch
+};
+
+struct alignas(16) BatchHeader {
+    uint32_t n_jobs, pad;
+    unsigned long long total_tiles;
+};
+
+BatchJob make_batch_job(const RenderLaunch& L);
+// Launches the persistent kernel over a job table already in device memory
+// (header followed by the jobs).  tile_w is the warp tile's width in pixels
+// (4, 8, 16 or 32; height 32/tile_w).
+cudaError_t launch_batch(const void* d_table, unsigned long long* d_queue, uint32_t* d_err, uint32_t tile_w,
+                         uint32_t block_threads, uint32_t blocks, uint32_t chunk, cudaStream_t stream);
+int batch_kernel_blocks_per_sm(uint32_t tile_w, uint32_t block_threads);
 
 }  // namespace xn

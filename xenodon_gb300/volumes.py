@@ -152,6 +152,63 @@ def _noise_fixed(xs, ys, zs, cell: float, seed: int, salt: int) -> torch.Tensor:
     return out
 
 
+def fire_ramp() -> np.ndarray:
+    """256-entry black -> red -> yellow -> white colour ramp (uint8, (256, 3))."""
+    t = np.arange(256) / 255.0
+    r = np.clip(3 * t, 0, 1)
+    g = np.clip(3 * t - 1, 0, 1)
+    b = np.clip(3 * t - 2, 0, 1)
+    return np.round(np.stack([r, g, b], 1) * 255).astype(np.uint8)
+
+
+def gas_field(n: int = 1024, seed: int = 2, slope: float = -2.5, zero_percentile: float = 60.0,
+              device=None, as_tensor: bool = False):
+    """Cosmology-like gas density (the TNG volume stand-in), n^3 RGBA8.
+
+    A Gaussian random field with power spectrum P(k) ~ k^slope, exponentiated
+    to a log-normal density, log10-mapped onto the 256-entry fire ramp; voxels
+    below the given percentile of the density are zeroed.  With as_tensor the
+    result stays on `device` as a torch uint8 tensor (n, n, n, 4)."""
+    dev = _device(device)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    kz = torch.fft.fftfreq(n, device=dev)
+    kx = torch.fft.rfftfreq(n, device=dev)
+    noise = torch.randn((n, n, n), generator=gen, device=dev, dtype=torch.float32)
+    spec = torch.fft.rfftn(noise)
+    del noise
+    for z0 in range(0, n, 64):  # scale by sqrt(P(k)) slab by slab to bound temporaries
+        z1 = min(n, z0 + 64)
+        k2 = kz[z0:z1, None, None] ** 2 + kz[None, :, None] ** 2 + kx[None, None, :] ** 2
+        amp = torch.where(k2 > 0, k2.clamp_min(1e-12) ** (slope / 4.0), torch.zeros_like(k2))
+        spec[z0:z1] *= amp
+    field = torch.fft.irfftn(spec, s=(n, n, n))
+    del spec
+    field = (field - field.mean()) / field.std()
+    # log10 of the log-normal density exp(field) is field / ln 10
+    logd = field / math.log(10.0)
+    del field
+    flat = logd.reshape(-1)
+    idx = torch.randint(0, flat.numel(), (1 << 22,), generator=gen, device=dev)
+    sample = flat[idx]
+    cut = torch.quantile(sample, zero_percentile / 100.0)
+    lo, hi = torch.quantile(sample, 0.001), torch.quantile(sample, 0.999)
+    ramp = torch.from_numpy(fire_ramp()).to(dev)
+    out = torch.empty((n, n, n, 4), dtype=torch.uint8, device=dev) if as_tensor else np.empty((n, n, n, 4), np.uint8)
+    for z0 in range(0, n, 64):
+        z1 = min(n, z0 + 64)
+        d = logd[z0:z1]
+        i = ((d - lo) / (hi - lo) * 255).clamp(0, 255).round().to(torch.int64)
+        rgb = ramp[i]
+        rgb[d < cut] = 0
+        blk = torch.cat([rgb, torch.full(rgb.shape[:-1] + (1,), 255, dtype=torch.uint8, device=dev)], dim=-1)
+        if as_tensor:
+            out[z0:z1] = blk
+        else:
+            out[z0:z1] = blk.cpu().numpy()
+    return out
+
+
 def random_grid(dz: int, dy: int, dx: int, seed: int = 0, density: float = 0.3, levels: int = 256) -> np.ndarray:
     """Small random test grid: `density` of voxels non-zero, alpha 255."""
     rng = np.random.default_rng(seed)
