@@ -10,7 +10,82 @@ import numpy as np
 import pytest
 
 
-def _classic_tiff(pages, photometric, spp, extra=None, big_endian=False, tile=None):
+def _lzw_encode(data: bytes) -> bytes:
+    """TIFF LZW, MSB-first: codes are written at the width the decoder reads
+    them with, which grows when its next free entry reaches 2^width - 1."""
+    def width(dec_next):
+        return 12 if dec_next >= 2047 else 11 if dec_next >= 1023 else 10 if dec_next >= 511 else 9
+
+    codes = []
+    table = {bytes([i]): i for i in range(256)}
+    next_code, dec_next, first = 258, 258, True
+    codes.append((256, 9))
+    w = b""
+    for c in data:
+        wc = w + bytes([c])
+        if wc in table:
+            w = wc
+            continue
+        codes.append((table[w], width(dec_next)))
+        if first:
+            first = False
+        else:
+            dec_next += 1
+        table[wc] = next_code
+        next_code += 1
+        w = bytes([c])
+        if next_code >= 4093:  # table full: clear, both sides start over
+            codes.append((256, width(dec_next)))
+            table = {bytes([i]): i for i in range(256)}
+            next_code, dec_next, first = 258, 258, True
+    if w:
+        codes.append((table[w], width(dec_next)))
+        if not first:
+            dec_next += 1
+    codes.append((257, width(dec_next)))
+    bits = "".join(format(c, f"0{n}b") for c, n in codes)
+    bits += "0" * (-len(bits) % 8)
+    return int(bits, 2).to_bytes(len(bits) // 8, "big") if bits else b""
+
+
+def _packbits_encode(data: bytes) -> bytes:
+    out = bytearray()
+    i = 0
+    while i < len(data):
+        run = 1
+        while i + run < len(data) and run < 128 and data[i + run] == data[i]:
+            run += 1
+        if run >= 3:
+            out += bytes([(257 - run) & 0xFF, data[i]])
+            i += run
+            continue
+        j = i
+        while j < len(data) and j - i < 128 and not (j + 2 < len(data) and data[j] == data[j + 1] == data[j + 2]):
+            j += 1
+        out += bytes([j - i - 1]) + data[i:j]
+        i = j
+    return bytes(out)
+
+
+def _encode_chunk(raw: bytes, compression: int, predictor: int, row_bytes: int, spp: int) -> bytes:
+    if predictor == 2:
+        a = np.frombuffer(raw, np.uint8).reshape(-1, row_bytes).astype(np.int32)
+        d = a.copy()
+        d[:, spp:] = a[:, spp:] - a[:, :-spp]
+        raw = (d & 0xFF).astype(np.uint8).tobytes()
+    if compression == 1:
+        return raw
+    if compression in (8, 32946):
+        return zlib.compress(raw, 6)
+    if compression == 5:
+        return _lzw_encode(raw)
+    if compression == 32773:
+        return _packbits_encode(raw)
+    raise ValueError(compression)
+
+
+def _classic_tiff(pages, photometric, spp, extra=None, big_endian=False, tile=None, compression=1, predictor=1,
+                  rows_per_strip=None):
     """Minimal independent TIFF writer: pages is a list of uint8 (h, w, spp)."""
     e = ">" if big_endian else "<"
     out = bytearray(b"MM" if big_endian else b"II")
@@ -28,10 +103,12 @@ def _classic_tiff(pages, photometric, spp, extra=None, big_endian=False, tile=No
                     t = np.zeros((th, tw, spp), np.uint8)
                     blk = img[j * th:(j + 1) * th, k * tw:(k + 1) * tw]
                     t[:blk.shape[0], :blk.shape[1]] = blk
-                    data_parts.append(t.tobytes())
+                    data_parts.append(_encode_chunk(t.tobytes(), compression, predictor, tw * spp, spp))
         else:
-            data_parts.append(img.tobytes())
-        n_entries = 10 + (1 if extra is not None else 0) + (1 if tile else 0)
+            rps = rows_per_strip or h
+            for y in range(0, h, rps):
+                data_parts.append(_encode_chunk(img[y:y + rps].tobytes(), compression, predictor, w * spp, spp))
+        n_entries = 10 + (1 if extra is not None else 0) + (1 if tile else 0) + (1 if predictor != 1 else 0)
         ifd_off = len(out)
         after_ifd = ifd_off + 2 + 12 * n_entries + 4
         bps_off = after_ifd
@@ -54,7 +131,7 @@ def _classic_tiff(pages, photometric, spp, extra=None, big_endian=False, tile=No
         entries.append(ent(256, 4, 1, w))
         entries.append(ent(257, 4, 1, h))
         entries.append(ent(258, 3, spp, bps_off) if spp > 2 else ent(258, 3, 1, 8))
-        entries.append(ent(259, 3, 1, 1))
+        entries.append(ent(259, 3, 1, compression))
         entries.append(ent(262, 3, 1, photometric))
         entries.append(ent(324 if tile else 273, 4, len(poffs), offs_off if len(poffs) > 1 else poffs[0]))
         entries.append(ent(277, 3, 1, spp))
@@ -62,11 +139,13 @@ def _classic_tiff(pages, photometric, spp, extra=None, big_endian=False, tile=No
             entries.append(ent(322, 3, 1, tile[0]))
             entries.append(ent(323, 3, 1, tile[1]))
         else:
-            entries.append(ent(278, 4, 1, h))
+            entries.append(ent(278, 4, 1, rows_per_strip or h))
         entries.append(ent(325 if tile else 279, 4, len(pcnts), cnt_off if len(pcnts) > 1 else pcnts[0]))
         entries.append(ent(284, 3, 1, 1))
         if extra is not None:
             entries.append(ent(338, 3, 1, extra))
+        if predictor != 1:
+            entries.append(ent(317, 3, 1, predictor))
         entries.sort(key=lambda b: struct.unpack(e + "H", b[:2])[0])
         assert len(entries) == n_entries
         out += struct.pack(e + "H", n_entries) + b"".join(entries) + struct.pack(e + "I", next_off)
@@ -194,3 +273,63 @@ def test_png_decodes_to_the_pixels(built_library, tmp_path, shape):
     img = np.random.default_rng(4).integers(0, 256, shape + (4,)).astype(np.uint8)
     xg.png_save(tmp_path / "f.png", img)
     assert np.array_equal(_png_decode((tmp_path / "f.png").read_bytes()), img)
+
+
+@pytest.mark.parametrize("compression", [5, 8, 32946, 32773])
+@pytest.mark.parametrize("predictor", [1, 2])
+@pytest.mark.parametrize("layout", ["strips", "tiles"])
+def test_tiff_compressed_pages_equal_uncompressed(built_library, tmp_path, compression, predictor, layout):
+    # LZW, Deflate and PackBits (+ the horizontal predictor), as libtiff
+    # decodes them for TIFFReadRGBAImage
+    import xenodon_gb300 as xg
+    rng = np.random.default_rng(7)
+    yy, xx = np.mgrid[0:37, 0:29]
+    pages = []
+    for z in range(3):
+        img = np.stack([(xx * 7 + z) % 256, (yy * 3) % 256, rng.integers(0, 4, (37, 29)) * 60], -1)
+        img[10:20] = 0  # runs
+        pages.append(img.astype(np.uint8))
+    kw = {"tile": (16, 16)} if layout == "tiles" else {"rows_per_strip": 5}
+    p = tmp_path / "c.tif"
+    p.write_bytes(_classic_tiff(pages, photometric=2, spp=3, compression=compression, predictor=predictor, **kw))
+    q = tmp_path / "u.tif"
+    q.write_bytes(_classic_tiff(pages, photometric=2, spp=3))
+    assert np.array_equal(xg.tiff_load(p), xg.tiff_load(q))
+
+
+def test_tiff_lzw_long_page_grows_the_code_width_and_clears(built_library, tmp_path):
+    # 64 KiB of noise: every code width 9..12 and at least one Clear code
+    import xenodon_gb300 as xg
+    rng = np.random.default_rng(8)
+    img = rng.integers(0, 256, (128, 128, 4)).astype(np.uint8)
+    p = tmp_path / "l.tif"
+    p.write_bytes(_classic_tiff([img], photometric=2, spp=4, extra=1, compression=5))
+    assert np.array_equal(xg.tiff_load(p)[0], img[::-1])
+
+
+@pytest.mark.parametrize("compression", [5, 8, 32773])
+def test_tiff_corrupt_compressed_strip_is_an_error(built_library, tmp_path, compression):
+    import xenodon_gb300 as xg
+    img = np.arange(8 * 8 * 3, dtype=np.uint8).reshape(8, 8, 3)
+    data = bytearray(_classic_tiff([img], photometric=2, spp=3, compression=compression))
+    good = _encode_chunk(img.tobytes(), compression, 1, 24, 3)
+    at = bytes(data).index(good)
+    data[at:at + len(good)] = good[: len(good) // 2] + bytes(len(good) - len(good) // 2)  # zeroed second half
+    p = tmp_path / "x.tif"
+    p.write_bytes(bytes(data))
+    with pytest.raises(xg.XenodonError) as e:
+        xg.tiff_load(p)
+    assert "corrupt compressed strip" in str(e.value)
+
+
+def test_tiff_unknown_compression_is_an_error(built_library, tmp_path):
+    import xenodon_gb300 as xg
+    img = np.zeros((4, 4, 3), np.uint8)
+    data = _classic_tiff([img], photometric=2, spp=3)
+    entry = struct.pack("<HHIHH", 259, 3, 1, 1, 0)
+    data = data.replace(entry, struct.pack("<HHIHH", 259, 3, 1, 7, 0))  # JPEG
+    p = tmp_path / "j.tif"
+    p.write_bytes(data)
+    with pytest.raises(xg.XenodonError) as e:
+        xg.tiff_load(p)
+    assert "compression 7 is not supported" in str(e.value)

@@ -277,3 +277,24 @@ def test_parity_empty_volume_and_degenerate_regions(ctx, trav):
         p, v = _params_pair(xg, c["w"], c["h"], out_off=c["out_off"], out_ext=(c["w"], c["h"]),
                             disp_off=c["disp_off"], disp_ext=c["disp_ext"])
         check_parity(ctx, trav, CAMS["inside"], p, v, grid=g, nodes=nodes, side=st["side"], label="empty")
+
+
+@pytest.mark.parametrize("trav", ("svo-df", "svo-naive"))
+@pytest.mark.parametrize("size", [(96, 64), (37, 23), (1, 1), (257, 3)])
+def test_ray_pool_equals_one_ray_per_thread(ctx, blob_volumes, monkeypatch, trav, size):
+    # svo-df and svo-naive run in the ray-pool kernel (lanes refill as rays
+    # finish); the one-ray-per-thread kernels must give the same bits, and
+    # both the oracle's
+    import xenodon_gb300 as xg
+    _, nodes, side = blob_volumes
+    vol = ctx.upload_svo(nodes, side)
+    p, v = _params_pair(xg, *size)
+    for cam in ("oblique", "inside", "grazing"):
+        pooled, _ = check_parity(ctx, trav, CAMS[cam], p, v, nodes=nodes, vol=vol, label=f"pool/{cam}")
+        _, em_pool, loads_pool = _gpu_counts(ctx, vol, trav, xg.make_camera(*CAMS[cam]), p)
+        monkeypatch.setenv("XN_RAY_POOL", "0")
+        plain, _, _ = ctx.render(vol, trav, xg.make_camera(*CAMS[cam]), p)
+        _, em_plain, loads_plain = _gpu_counts(ctx, vol, trav, xg.make_camera(*CAMS[cam]), p)
+        monkeypatch.delenv("XN_RAY_POOL")
+        assert np.array_equal(pooled, plain), cam
+        assert np.array_equal(em_pool, em_plain) and np.array_equal(loads_pool, loads_plain), cam

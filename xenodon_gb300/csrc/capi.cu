@@ -469,6 +469,11 @@ int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_p
         L.inner_depth = v->inner_depth;
         L.leaves = v->leaves;
         L.depth_consistent = v->depth_consistent;
+        // svo-df and svo-naive through the ray-pool kernel unless
+        // XN_RAY_POOL=0 (same results; the switch keeps the one-ray-per-thread
+        // kernels reachable)
+        const char* pool = std::getenv("XN_RAY_POOL");
+        L.pool = !(pool && pool[0] == '0');
     }
     for (int i = 0; i < 3; ++i) L.dim[i] = v->dim[i];
     return XN_OK;

@@ -2,9 +2,13 @@
 //
 // Stacked TIFF (Grid::load_tiff, src/model/Grid.cpp:27-79).  libtiff is not
 // available, so this is a reader of its own for the files the reference's
-// tools write (tifffile: classic or BigTIFF, one page per z slice,
-// uncompressed, 8-bit gray / RGB / RGBA, strips or tiles, contiguous
-// samples).  It returns what TIFFReadRGBAImage hands the reference:
+// tools write (tifffile: classic or BigTIFF, one page per z slice, 8-bit
+// gray / RGB / RGBA, strips or tiles, contiguous samples), uncompressed or
+// with the codecs libtiff decodes for such files: LZW (5, libtiff's MSB-first
+// form with the code width growing one code early), Deflate (8 and the old
+// 32946; zlib streams, inflated by an RFC 1950/1951 decoder of its own) and
+// PackBits (32773), each optionally with the horizontal predictor (2).  It
+// returns what TIFFReadRGBAImage hands the reference:
 //   - rows bottom-up: grid row y of a layer is image row height-1-y
 //     (TIFFReadRGBAImage's default ORIENTATION_BOTLEFT raster);
 //   - gray -> R=G=B=gray, A=255; RGB -> A=255;
@@ -60,6 +64,7 @@ struct Ifd {
     uint32_t width = 0, height = 0;
     uint16_t bits = 1, spp = 1, compression = 1, photometric = 1, planar = 1;
     uint16_t extra = 0;  // first ExtraSamples value
+    uint16_t predictor = 1;
     uint32_t rows_per_strip = 0xFFFFFFFFu;
     uint32_t tile_w = 0, tile_h = 0;
     std::vector<uint64_t> offsets, counts;
@@ -103,7 +108,7 @@ int read_ifd(Reader& r, uint64_t off, Ifd& d, const char* path) {
         std::vector<uint64_t> v;
         switch (tag) {
         case 256: case 257: case 258: case 259: case 262: case 273: case 277: case 278: case 279:
-        case 284: case 322: case 323: case 324: case 325: case 338:
+        case 284: case 317: case 322: case 323: case 324: case 325: case 338:
             if (!entry_values(r, e, v) || v.empty()) return fail(XN_ERR_FORMAT, "'%s': bad value of tag %u", path, tag);
             break;
         default:
@@ -124,6 +129,7 @@ int read_ifd(Reader& r, uint64_t off, Ifd& d, const char* path) {
         case 278: d.rows_per_strip = (uint32_t)std::min<uint64_t>(v[0], 0xFFFFFFFFu); break;
         case 279: case 325: d.counts = v; break;
         case 284: d.planar = (uint16_t)v[0]; break;
+        case 317: d.predictor = (uint16_t)v[0]; break;
         case 322: d.tile_w = (uint32_t)v[0]; break;
         case 323: d.tile_h = (uint32_t)v[0]; break;
         case 338: d.extra = (uint16_t)v[0]; break;
@@ -133,9 +139,316 @@ int read_ifd(Reader& r, uint64_t off, Ifd& d, const char* path) {
     return XN_OK;
 }
 
+// ------------------------------------------------------------- codecs ---
+
+// Inflate (RFC 1951) with 15-bit lookup tables: each table entry holds the
+// symbol and the code length for every 15-bit window whose low bits start
+// with that code (deflate packs Huffman codes most-significant bit first
+// into a least-significant-bit-first stream, so codes are bit-reversed).
+struct BitIn {
+    const uint8_t* p;
+    size_t n, pos = 0;
+    uint64_t buf = 0, used = 0;  // used: bits consumed
+    int cnt = 0;                 // bits in buf (bytes past the end read as 0)
+    BitIn(const uint8_t* d, size_t len) : p(d), n(len) {}
+    uint32_t peek(int k) {
+        while (cnt <= 56) {
+            buf |= (uint64_t)(pos < n ? p[pos] : 0) << cnt;
+            ++pos;
+            cnt += 8;
+        }
+        return (uint32_t)(buf & ((1ull << k) - 1));
+    }
+    void skip(int k) {
+        buf >>= k;
+        cnt -= k;
+        used += (uint64_t)k;
+    }
+    uint32_t bits(int k) {
+        if (k == 0) return 0;
+        const uint32_t v = peek(k);
+        skip(k);
+        return v;
+    }
+    bool over() const { return used > (uint64_t)n * 8; }
+    void align() { skip((int)((8 - (used & 7)) & 7)); }
+};
+
+struct Huffman {
+    std::vector<uint32_t> table;  // symbol << 4 | length, 0 = no code
+    bool build(const uint8_t* lengths, int n) {
+        uint16_t count[16] = {0};
+        for (int i = 0; i < n; ++i) ++count[lengths[i]];
+        count[0] = 0;
+        int left = 1;
+        for (int l = 1; l < 16; ++l) {
+            left = (left << 1) - count[l];
+            if (left < 0) return false;  // over-subscribed
+        }
+        uint32_t next[16];
+        uint32_t code = 0;
+        for (int l = 1; l < 16; ++l) {
+            code = (code + count[l - 1]) << 1;
+            next[l] = code;
+        }
+        table.assign(1u << 15, 0u);
+        for (int s = 0; s < n; ++s) {
+            const int l = lengths[s];
+            if (!l) continue;
+            const uint32_t c = next[l]++;
+            uint32_t r = 0;
+            for (int b = 0; b < l; ++b) r |= ((c >> b) & 1u) << (l - 1 - b);
+            for (uint32_t k = r; k < (1u << 15); k += 1u << l) table[k] = ((uint32_t)s << 4) | (uint32_t)l;
+        }
+        return true;
+    }
+    int decode(BitIn& in) const {
+        const uint32_t e = table[in.peek(15)];
+        if (!e) return -1;
+        in.skip((int)(e & 15u));
+        return (int)(e >> 4);
+    }
+};
+
+const uint16_t LEN_BASE[29] = {3, 4, 5, 6, 7, 8, 9, 10, 11, 13, 15, 17, 19, 23, 27, 31,
+                               35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
+const uint8_t LEN_EXTRA[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
+const uint16_t DIST_BASE[30] = {1, 2, 3, 4, 5, 7, 9, 13, 17, 25, 33, 49, 65, 97, 129,
+                                193, 257, 385, 513, 769, 1025, 1537, 2049, 3073, 4097, 6145, 8193, 12289, 16385, 24577};
+const uint8_t DIST_EXTRA[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6, 6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+
+// Inflates a zlib stream into out (exactly out.size() bytes expected).
+bool inflate_zlib(const uint8_t* src, size_t n, std::vector<uint8_t>& out) {
+    if (n < 2) return false;
+    const uint32_t cmf = src[0], flg = src[1];
+    if ((cmf & 15u) != 8 || ((cmf << 8) | flg) % 31 != 0 || (flg & 0x20)) return false;
+    BitIn in(src + 2, n - 2);
+    size_t o = 0;
+    const size_t cap = out.size();
+    Huffman lit, dist;
+    for (;;) {
+        const uint32_t last = in.bits(1);
+        const uint32_t type = in.bits(2);
+        if (type == 0) {
+            in.align();
+            const uint32_t len = in.bits(16), nlen = in.bits(16);
+            if ((len ^ 0xFFFFu) != nlen) return false;
+            for (uint32_t i = 0; i < len; ++i) {
+                if (o >= cap) return false;
+                out[o++] = (uint8_t)in.bits(8);
+            }
+        } else if (type == 1 || type == 2) {
+            uint8_t lengths[320];
+            int nlit = 288, ndist = 30;
+            if (type == 1) {
+                for (int i = 0; i < 144; ++i) lengths[i] = 8;
+                for (int i = 144; i < 256; ++i) lengths[i] = 9;
+                for (int i = 256; i < 280; ++i) lengths[i] = 7;
+                for (int i = 280; i < 288; ++i) lengths[i] = 8;
+                for (int i = 0; i < 30; ++i) lengths[288 + i] = 5;
+            } else {
+                nlit = (int)in.bits(5) + 257;
+                ndist = (int)in.bits(5) + 1;
+                const int ncode = (int)in.bits(4) + 4;
+                static const uint8_t ORDER[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+                uint8_t cl[19] = {0};
+                for (int i = 0; i < ncode; ++i) cl[ORDER[i]] = (uint8_t)in.bits(3);
+                Huffman clh;
+                if (nlit > 286 || ndist > 30 || !clh.build(cl, 19)) return false;
+                int i = 0;
+                while (i < nlit + ndist) {
+                    const int sym = clh.decode(in);
+                    if (sym < 0) return false;
+                    if (sym < 16) { lengths[i++] = (uint8_t)sym; continue; }
+                    int rep = 0;
+                    uint8_t val = 0;
+                    if (sym == 16) {
+                        if (i == 0) return false;
+                        val = lengths[i - 1];
+                        rep = 3 + (int)in.bits(2);
+                    } else if (sym == 17) {
+                        rep = 3 + (int)in.bits(3);
+                    } else {
+                        rep = 11 + (int)in.bits(7);
+                    }
+                    if (i + rep > nlit + ndist) return false;
+                    while (rep--) lengths[i++] = val;
+                }
+                if (lengths[256] == 0) return false;
+                // the distance lengths follow the literal lengths directly
+                std::memmove(lengths + 288, lengths + nlit, (size_t)ndist);
+                for (int k = nlit; k < 288; ++k) lengths[k] = 0;
+            }
+            if (!lit.build(lengths, 288) || !dist.build(lengths + 288, ndist)) return false;
+            for (;;) {
+                const int sym = lit.decode(in);
+                if (sym < 0 || in.over()) return false;
+                if (sym < 256) {
+                    if (o >= cap) return false;
+                    out[o++] = (uint8_t)sym;
+                } else if (sym == 256) {
+                    break;
+                } else {
+                    const int li = sym - 257;
+                    if (li >= 29) return false;
+                    const uint32_t len = LEN_BASE[li] + in.bits(LEN_EXTRA[li]);
+                    const int di = dist.decode(in);
+                    if (di < 0 || di >= 30) return false;
+                    const uint32_t d = DIST_BASE[di] + in.bits(DIST_EXTRA[di]);
+                    if (d > o || len > cap - o) return false;
+                    for (uint32_t k = 0; k < len; ++k, ++o) out[o] = out[o - d];
+                }
+            }
+        } else {
+            return false;
+        }
+        if (in.over()) return false;
+        if (last) break;
+    }
+    if (o != cap) return false;
+    // zlib trailer: Adler-32 of the output, big-endian (zlib reports a mismatch as an error)
+    in.align();
+    uint32_t want = 0;
+    for (int k = 0; k < 4; ++k) want = (want << 8) | in.bits(8);
+    if (in.over()) return false;
+    uint32_t a = 1, b = 0;
+    for (size_t k = 0; k < o; ++k) {
+        a = (a + out[k]) % 65521u;
+        b = (b + a) % 65521u;
+    }
+    return ((b << 16) | a) == want;
+}
+
+// TIFF LZW (compression 5): MSB-first codes of 9..12 bits, Clear = 256,
+// EndOfInformation = 257; the width grows when the next free entry reaches
+// 2^width - 1 (one code early, as libtiff's decoder and every TIFF writer do).
+bool lzw_decode(const uint8_t* src, size_t n, std::vector<uint8_t>& out) {
+    const size_t cap = out.size();
+    std::vector<uint16_t> prefix(4096), len(4096);
+    std::vector<uint8_t> suffix(4096), first(4096);
+    for (int i = 0; i < 256; ++i) {
+        prefix[i] = 0xFFFF;
+        suffix[i] = first[i] = (uint8_t)i;
+        len[i] = 1;
+    }
+    size_t o = 0;
+    uint64_t bitpos = 0;
+    const uint64_t nbits_total = (uint64_t)n * 8;
+    int width = 9;
+    uint32_t next = 258;
+    int old = -1;
+    auto emit = [&](uint32_t code) -> bool {
+        const uint32_t l = len[code];
+        if (l > cap - o) return false;
+        uint32_t c = code;
+        for (uint32_t k = l; k-- > 0;) {
+            out[o + k] = suffix[c];
+            c = prefix[c];
+        }
+        o += l;
+        return true;
+    };
+    while (bitpos + width <= nbits_total) {
+        uint32_t code = 0;
+        for (int b = 0; b < width; ++b, ++bitpos) code = (code << 1) | ((src[bitpos >> 3] >> (7 - (bitpos & 7))) & 1u);
+        if (code == 257) break;
+        if (code == 256) {
+            width = 9;
+            next = 258;
+            old = -1;
+            continue;
+        }
+        if (old < 0) {
+            if (code > 255 || !emit(code)) return false;
+            old = (int)code;
+            continue;
+        }
+        uint8_t head;
+        if (code < next) {
+            if (!emit(code)) return false;
+            head = first[code];
+        } else if (code == next && next < 4096) {
+            head = first[old];
+            // the new entry is old's string plus its own first byte
+            const uint32_t l = len[old];
+            if (l + 1 > cap - o) return false;
+            const size_t start = o;
+            if (!emit((uint32_t)old)) return false;
+            out[start + l] = head;
+            ++o;
+        } else {
+            return false;
+        }
+        if (next < 4096) {
+            prefix[next] = (uint16_t)old;
+            suffix[next] = head;
+            first[next] = first[old];
+            len[next] = (uint16_t)(len[old] + 1);
+            ++next;
+            if (next >= 2047) width = 12;
+            else if (next >= 1023) width = 11;
+            else if (next >= 511) width = 10;
+        }
+        old = (int)code;
+    }
+    return o == cap;
+}
+
+// PackBits (compression 32773): a signed header byte h; 0..127 copies the
+// next h+1 bytes, -127..-1 repeats the next byte 1-h times, -128 is skipped.
+bool packbits_decode(const uint8_t* src, size_t n, std::vector<uint8_t>& out) {
+    const size_t cap = out.size();
+    size_t i = 0, o = 0;
+    while (i < n && o < cap) {
+        const int h = (int)(int8_t)src[i++];
+        if (h >= 0) {
+            const size_t k = (size_t)h + 1;
+            if (k > n - i || k > cap - o) return false;
+            std::memcpy(&out[o], &src[i], k);
+            i += k;
+            o += k;
+        } else if (h != -128) {
+            const size_t k = (size_t)(1 - h);
+            if (i >= n || k > cap - o) return false;
+            std::memset(&out[o], src[i++], k);
+            o += k;
+        }
+    }
+    return o == cap;
+}
+
+// Reads one strip or tile (bytes stored at off, count of them) and decodes it
+// into out (its uncompressed size); row_bytes = one row of the strip / tile.
+int read_chunk(Reader& r, const Ifd& d, uint64_t off, uint64_t count, std::vector<uint8_t>& out, uint64_t row_bytes,
+               const char* path, const char* what) {
+    if (d.compression == 1) {
+        if (!r.read_at(off, out.data(), out.size())) return fail(XN_ERR_FORMAT, "'%s': truncated %s", path, what);
+    } else {
+        std::vector<uint8_t> raw(count ? count : 1);
+        if (!count || !r.read_at(off, raw.data(), count)) return fail(XN_ERR_FORMAT, "'%s': truncated %s", path, what);
+        bool ok;
+        if (d.compression == 5) ok = lzw_decode(raw.data(), count, out);
+        else if (d.compression == 8 || d.compression == 32946) ok = inflate_zlib(raw.data(), count, out);
+        else ok = packbits_decode(raw.data(), count, out);
+        if (!ok) return fail(XN_ERR_FORMAT, "'%s': corrupt compressed %s (compression %u)", path, what, d.compression);
+    }
+    if (d.predictor == 2) {
+        // horizontal differencing: each sample is stored minus the same sample of the previous pixel
+        for (uint64_t row = 0; row + row_bytes <= out.size(); row += row_bytes)
+            for (uint64_t i = d.spp; i < row_bytes; ++i) out[row + i] = (uint8_t)(out[row + i] + out[row + i - d.spp]);
+    }
+    return XN_OK;
+}
+
 // Decodes one page into RGBA rows, bottom-up (TIFFReadRGBAImage's raster).
 int decode_page(Reader& r, const Ifd& d, uint32_t width, uint32_t height, uint8_t* out, const char* path) {
-    if (d.compression != 1) return fail(XN_ERR_FORMAT, "'%s': compressed TIFF (compression %u) is not supported", path, d.compression);
+    if (d.compression != 1 && d.compression != 5 && d.compression != 8 && d.compression != 32946 &&
+        d.compression != 32773)
+        return fail(XN_ERR_FORMAT, "'%s': TIFF compression %u is not supported", path, d.compression);
+    if (d.predictor != 1 && d.predictor != 2)
+        return fail(XN_ERR_FORMAT, "'%s': TIFF predictor %u is not supported", path, d.predictor);
+    if (d.compression != 1 && d.counts.size() < d.offsets.size())
+        return fail(XN_ERR_FORMAT, "'%s': compressed TIFF without byte counts", path);
     if (d.bits != 8) return fail(XN_ERR_FORMAT, "'%s': only 8-bit samples are supported (got %u)", path, d.bits);
     if (d.planar != 1 && d.spp > 1) return fail(XN_ERR_FORMAT, "'%s': planar TIFF is not supported", path);
     const bool gray = d.photometric == 0 || d.photometric == 1;
@@ -153,8 +466,10 @@ int decode_page(Reader& r, const Ifd& d, uint32_t width, uint32_t height, uint8_
         std::vector<uint8_t> tile((uint64_t)d.tile_w * d.tile_h * spp);
         for (uint32_t j = 0; j < ty; ++j)
             for (uint32_t i = 0; i < tx; ++i) {
-                if (!r.read_at(d.offsets[(uint64_t)j * tx + i], tile.data(), tile.size()))
-                    return fail(XN_ERR_FORMAT, "'%s': truncated tile", path);
+                const uint64_t t = (uint64_t)j * tx + i;
+                const int rc = read_chunk(r, d, d.offsets[t], t < d.counts.size() ? d.counts[t] : 0, tile,
+                                          (uint64_t)d.tile_w * spp, path, "tile");
+                if (rc) return rc;
                 for (uint32_t y = 0; y < d.tile_h && j * d.tile_h + y < d.height; ++y) {
                     const uint32_t w = std::min(d.tile_w, d.width - i * d.tile_w);
                     std::memcpy(&px[(((uint64_t)(j * d.tile_h + y)) * d.width + i * d.tile_w) * spp],
@@ -165,10 +480,14 @@ int decode_page(Reader& r, const Ifd& d, uint32_t width, uint32_t height, uint8_
         const uint64_t rps = std::min<uint64_t>(d.rows_per_strip ? d.rows_per_strip : 1, d.height);
         const uint64_t strips = (d.height + rps - 1) / rps;
         if (d.offsets.size() < strips) return fail(XN_ERR_FORMAT, "'%s': missing strips", path);
+        std::vector<uint8_t> strip;
         for (uint64_t s = 0; s < strips; ++s) {
             const uint64_t rows = std::min<uint64_t>(rps, d.height - s * rps);
-            if (!r.read_at(d.offsets[s], &px[s * rps * d.width * spp], rows * d.width * spp))
-                return fail(XN_ERR_FORMAT, "'%s': truncated strip", path);
+            strip.resize(rows * d.width * spp);
+            const int rc = read_chunk(r, d, d.offsets[s], s < d.counts.size() ? d.counts[s] : 0, strip,
+                                      (uint64_t)d.width * spp, path, "strip");
+            if (rc) return rc;
+            std::memcpy(&px[s * rps * d.width * spp], strip.data(), strip.size());
         }
     }
     for (uint32_t y = 0; y < height; ++y) {

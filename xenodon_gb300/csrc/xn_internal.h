@@ -45,6 +45,7 @@ struct RenderLaunch {
     const uint32_t* inner_depth;
     const uint32_t* leaves;
     int depth_consistent;         // every internal node's depth field = its depth in the tree
+    int pool;                     // svo-df / svo-naive through the ray-pool kernel (lanes refill as rays finish)
     // outputs (device pointers)
     void* d_rgba;
     float* d_emission;
