@@ -72,8 +72,11 @@ uint32_t resident_blocks(Ctx* c, const xn_batch_config& cfg) {
 
 xn_batch_config default_config() { return xn_batch_config{8, 128, 0, 1}; }
 
-// Job-table buffers of a context for xn_render_batch.
-int ensure_batch_buffers(Ctx* c, uint64_t bytes) {
+// Pinned staging for the job tables of xn_render_batch (one per context; a
+// new table is written only after the previous one was copied out).
+int ensure_batch_staging(Ctx* c, uint64_t bytes) {
+    if (!c->batch_copied && cudaEventCreateWithFlags(&c->batch_copied, cudaEventDisableTiming) != cudaSuccess)
+        return fail(XN_ERR_CUDA, "batch: event");
     if (c->batch_host_bytes < bytes) {
         if (c->batch_host) {
             cudaEventSynchronize(c->batch_copied);
@@ -85,33 +88,32 @@ int ensure_batch_buffers(Ctx* c, uint64_t bytes) {
             return fail(XN_ERR_NOMEM, "batch: pinned job table");
         c->batch_host_bytes = bytes;
     }
-    if (c->batch_table.bytes < bytes) {
-        cudaDeviceSynchronize();  // the previous table may still be read
-        int r = c->ensure_buffer(c->batch_table, bytes, "batch: job table");
-        if (r) return r;
-    }
-    if (!c->batch_queue.ptr) {
-        int r = c->ensure_buffer(c->batch_queue, 64, "batch: work queue");
-        if (r) return r;
-    }
-    if (!c->batch_copied && cudaEventCreateWithFlags(&c->batch_copied, cudaEventDisableTiming) != cudaSuccess)
-        return fail(XN_ERR_CUDA, "batch: event");
     return XN_OK;
 }
 
+// Every launch gets a device job table and work counter of its own, allocated
+// and freed in the order of its stream: launches on other streams (the render
+// server runs several) never see them, and no launch waits for another.
 int render_batch_locked(Ctx* c, const xn_job* jobs, int n, const xn_batch_config& cfg, cudaStream_t s) {
     const uint64_t cap = sizeof(BatchHeader) + (uint64_t)n * sizeof(BatchJob);
-    int r = ensure_batch_buffers(c, cap);
+    int r = ensure_batch_staging(c, cap);
     if (r) return r;
-    cudaEventSynchronize(c->batch_copied);  // the staging table of the previous batch was copied
+    cudaError_t e = cudaEventSynchronize(c->batch_copied);  // the previous table left the staging buffer
+    if (e != cudaSuccess) return cuda_fail(e, "xn_render_batch: staging");
     uint64_t bytes = 0;
     if ((r = fill_table(c, jobs, n, cfg.tile_width, c->batch_host, c->batch_host_bytes, &bytes))) return r;
-    cudaError_t e = cudaMemcpyAsync(c->batch_table.ptr, c->batch_host, bytes, cudaMemcpyHostToDevice, s);
+    const uint64_t queue_off = (bytes + 255) & ~255ull;
+    void* d = nullptr;
+    e = cudaMallocAsync(&d, queue_off + 256, s);
+    if (e != cudaSuccess) return cuda_fail(e, "xn_render_batch: job table");
+    unsigned long long* queue = reinterpret_cast<unsigned long long*>(static_cast<char*>(d) + queue_off);
+    e = cudaMemcpyAsync(d, c->batch_host, bytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaEventRecord(c->batch_copied, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(c->batch_queue.ptr, 0, 8, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(queue, 0, 8, s);
     if (e == cudaSuccess)
-        e = launch_batch(c->batch_table.ptr, static_cast<unsigned long long*>(c->batch_queue.ptr), c->d_err,
-                         cfg.tile_width, cfg.block_threads, resident_blocks(c, cfg), cfg.chunk, s);
+        e = launch_batch(d, queue, c->d_err, cfg.tile_width, cfg.block_threads, resident_blocks(c, cfg), cfg.chunk, s);
+    const cudaError_t ef = cudaFreeAsync(d, s);
+    if (e == cudaSuccess) e = ef;
     return e == cudaSuccess ? XN_OK : cuda_fail(e, "xn_render_batch");
 }
 

@@ -80,8 +80,6 @@ void Ctx::release_extra() {
         cudaEventDestroy(batch_copied);
     }
     if (batch_host) cudaFreeHost(batch_host);
-    device_free(batch_table.ptr, batch_table.bytes);
-    device_free(batch_queue.ptr, batch_queue.bytes);
 }
 
 int Ctx::activate() {

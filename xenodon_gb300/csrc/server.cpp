@@ -145,8 +145,25 @@ int xn_server::make_resident(uint32_t id, ServerVolume& v, const std::vector<uin
 bool xn_server::retire_finished() {
     bool any_retired = false;
     for (auto& slot : slots) {
-        if (!slot.busy || cudaEventQuery(slot.done) != cudaSuccess) continue;
+        if (!slot.busy) continue;
+        const cudaError_t q_state = cudaEventQuery(slot.done);
+        if (q_state == cudaErrorNotReady) continue;
         const auto now = Clock::now();
+        if (q_state != cudaSuccess) {
+            // the batch failed on the device: its requests fail, the slot is free again
+            for (Request* q : slot.reqs) {
+                cudaFreeAsync(q->d_out, slot.stream);
+                q->d_out = nullptr;
+                used -= q->out_bytes;
+                volumes[q->volume_id].refs--;
+                q->status = XN_ERR_CUDA;
+                ++failed;
+            }
+            slot.reqs.clear();
+            slot.busy = false;
+            any_retired = true;
+            continue;
+        }
         for (Request* q : slot.reqs) {
             std::memcpy(q->out, static_cast<uint8_t*>(slot.staging) + q->staging_off, q->out_bytes);
             cudaFreeAsync(q->d_out, slot.stream);  // stream-ordered: no device-wide synchronisation

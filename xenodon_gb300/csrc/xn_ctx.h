@@ -31,7 +31,6 @@ struct Ctx {
     int sms = 0;
     void* batch_host = nullptr;  // pinned job table
     uint64_t batch_host_bytes = 0;
-    DeviceBuffer batch_table, batch_queue;
     cudaEvent_t batch_copied = nullptr;
     xn_batch_config tuned[32] = {};
     int tuned_valid[32] = {};
