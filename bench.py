@@ -277,13 +277,16 @@ def measure_batched(ctx, xg, args):
     }
 
 
-def measure_dda_4k(ctx, xg, g, n):
+def measure_dda_4k(ctx, xg, g, n, vol=None):
     """Plain DDA on the n^3 gas-field grid at 3840x2160 from 8 orbit cameras at
     2x the extent: Mrays/s and the fraction of the HBM roofline (4 B per texel
-    the reference reads + 4 B per pixel, over the measured HBM copy bandwidth)."""
+    the reference reads + 4 B per pixel, over the measured HBM copy bandwidth).
+    `vol`: an already resident grid volume (kept), else one is made from g."""
     import torch
     from xenodon_gb300 import cameras
-    vol = ctx.upload_grid_device(g.data_ptr(), (n, n, n))
+    own = vol is None
+    if own:
+        vol = ctx.upload_grid_device(g.data_ptr(), (n, n, n))
     w, h = 3840, 2160
     params = xg.make_params(w, h, EMISSION)
     cams = [xg.make_camera(*c) for c in cameras.orbit(np.array([0.5, 0.5, 0.5]), 2.0, 8)]
@@ -306,7 +309,8 @@ def measure_dda_4k(ctx, xg, g, n):
         ctx.render_device(vol, "dda", c, params, out.data_ptr(), None, loads.data_ptr(), sptr)
         words += int(loads.to(torch.int64).sum().item())
     torch.cuda.synchronize()
-    vol.release()
+    if own:
+        vol.release()
     total_ms = sum(ms)
     alg = 4.0 * words + 4.0 * w * h * len(cams)
     gbs = alg / (total_ms * 1e-3) / 1e9
@@ -315,6 +319,94 @@ def measure_dda_4k(ctx, xg, g, n):
             "ms_per_frame": round(total_ms / len(cams), 4), "mrays_s": round(w * h * len(cams) / (total_ms * 1e3), 1),
             "algorithmic_gbs": round(gbs, 1), "hbm_frac": round(gbs / peak, 4),
             "texels_per_ray": round(words / (w * h * len(cams)), 1)}
+
+
+def measure_c3(ctx, xg, args):
+    """The 2048^3 workload: a 32 GiB gas-field grid (seed 3, the 1024^3
+    recipe) and its octree, DDA and esvo at 3840x2160 along a 150-frame orbit
+    at 2x the extent; one launch per frame vs the autotuned persistent batch.
+
+    The octree has about 0.93 nodes per voxel (8e9 here), beyond the 32-bit
+    indices of the reference's node array and beyond HBM at 40 bytes a node,
+    so it is built lean: straight into the device layout (36 bytes per
+    internal node, leaf colours inline), which esvo reads."""
+    import torch
+    from xenodon_gb300 import cameras, volumes
+    n = args.c3_size
+    free, _ = torch.cuda.mem_get_info()
+    need = 5 * n ** 3 * 4 * 1.3  # field generation temporaries dominate
+    if free < need:
+        return {"skipped": f"{free / 2**30:.0f} GiB free, {need / 2**30:.0f} GiB wanted"}
+    t0 = time.time()
+    g = volumes.gas_field(n, seed=3, device="cuda", as_tensor=True)
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    gen_s = time.time() - t0
+    t0 = time.time()
+    grid_vol = ctx.upload_grid_device(g.data_ptr(), (n, n, n))
+    upload_s = time.time() - t0
+    t0 = time.time()
+    svo_vol, st = ctx.build_svo_volume(g.data_ptr(), (n, n, n), "sparse", lean=True)
+    build_s = time.time() - t0
+    del g
+    torch.cuda.empty_cache()
+    w, h = 3840, 2160
+    params = xg.make_params(w, h, EMISSION)
+    path = cameras.orbit(np.array([0.5, 0.5, 0.5]), 2.0, 150)
+    frames = path[:: max(1, len(path) // args.c3_frames)][: args.c3_frames]
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    result = {"workload": f"{n}^3 gas field (seed 3) grid + lean sparse octree, dda and esvo at {w}x{h}, "
+                          f"{len(frames)} frames of a 150-frame orbit at 2x the extent",
+              "field_gen_s": round(gen_s, 2), "texture_upload_s": round(upload_s, 2),
+              "octree_build_s": round(build_s, 2), "octree_nodes": st["n_nodes"],
+              "octree_device_bytes": svo_vol.info()["device_bytes"], "octree_depth": st["depth"]}
+    result["dda_4k"] = measure_dda_4k(ctx, xg, None, n, vol=grid_vol)
+
+    def timed(fn, reps=2):
+        fn()
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        return best
+
+    for trav, vol in (("dda", grid_vol), ("esvo", svo_vol)):
+        specs = [(vol, trav, xg.make_camera(*c), params) for c in frames]
+        bufs = [torch.empty((h, w), dtype=torch.int32, device="cuda") for _ in specs]
+
+        def plain():
+            for (v, t, c, p), b in zip(specs, bufs):
+                ctx.render_device(v, t, c, p, b.data_ptr(), None, None, sptr)
+
+        plain_ms = timed(plain)
+        keep = [b.clone() for b in bufs[::4]]
+        jobs = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs, bufs))
+        untuned_ms = timed(lambda: ctx.render_batch(jobs, len(specs), xg.BatchConfig(8, 128, 0, 1), sptr), reps=1)
+        k = min(4, len(specs))
+        tune = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs[:: len(specs) // k], bufs))
+        best, _ = ctx.autotune_batch(tune, k, sptr)
+        for b in bufs:
+            b.fill_(-1)
+        tuned_ms = timed(lambda: ctx.render_batch(jobs, len(specs), best, sptr))
+        same = all(torch.equal(a, b) for a, b in zip(keep, bufs[::4]))
+        rays = w * h * len(specs)
+        result[trav] = {"plain_mrays_s": round(rays / (plain_ms * 1e3), 1),
+                        "batch_untuned_mrays_s": round(rays / (untuned_ms * 1e3), 1),
+                        "batch_autotuned_mrays_s": round(rays / (tuned_ms * 1e3), 1),
+                        "autotuned_vs_plain": round(plain_ms / tuned_ms, 3), "launch_shape": best.as_dict(),
+                        "identical_images": bool(same)}
+        del bufs, keep
+    svo_vol.release()
+    grid_vol.release()
+    torch.cuda.empty_cache()
+    return result
 
 
 def measure_serving(ctx, xg, args, scene):
@@ -519,8 +611,11 @@ def run_ours(args):
         "build": {"svo_build_s": round(build_s, 3), "volume_gen_s": round(gen_s, 2)},
     }
     if rank == 0 and not args.no_extras:
-        for key, fn in (("batched", lambda: measure_batched(ctx, xg, args)),
-                        ("serving", lambda: measure_serving(ctx, xg, args, (grid, nodes, st["side"])))):
+        extras = [("batched", lambda: measure_batched(ctx, xg, args)),
+                  ("serving", lambda: measure_serving(ctx, xg, args, (grid, nodes, st["side"])))]
+        if args.c3_size:
+            extras.append(("large", lambda: measure_c3(ctx, xg, args)))
+        for key, fn in extras:
             try:
                 line[key] = fn()
             except Exception as exc:  # the headline line is printed regardless
@@ -554,6 +649,8 @@ def main(argv=None):
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and serving measurements")
     ap.add_argument("--batched-size", type=int, default=1024)
     ap.add_argument("--batched-cameras", type=int, default=64)
+    ap.add_argument("--c3-size", type=int, default=2048, help="grid size of the large workload (0: skip it)")
+    ap.add_argument("--c3-frames", type=int, default=16)
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 200.0, 1000.0, 0.0])
     args = ap.parse_args(argv)

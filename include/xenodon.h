@@ -256,7 +256,16 @@ XN_API void xn_free(void* p);
 /* `xenodon convert` followed by an upload, without leaving the device: builds
  * the octree of a grid in device memory (d_rgba: packed RGBA8 texels, x
  * fastest) and makes it a resident volume.  The node array is the one
- * xn_build_svo returns. */
+ * xn_build_svo returns.
+ *
+ * type | XN_BUILD_LEAN (sparse trees only) writes the device layout directly
+ * and never holds the 40-byte node array: about 36 bytes per internal node
+ * instead of 40 per node plus the layout, so grids whose trees exceed 2^32
+ * nodes (the node array's index range) still build, as long as they have
+ * fewer than 2^31 internal nodes.  The volume renders every traversal but
+ * svo-rope (it has no rope records) with the same results as the full build;
+ * the stats are the same as well. */
+#define XN_BUILD_LEAN 0x100
 XN_API int xn_build_svo_volume(xn_ctx* ctx, const void* d_rgba, uint32_t dx, uint32_t dy, uint32_t dz, int type,
                                int heuristic, double threshold, xn_volume** out, xn_build_stats* stats);
 

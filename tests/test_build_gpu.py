@@ -126,3 +126,59 @@ def test_device_resident_build_and_upload_match_host_paths(ctx):
     a, _, _ = ctx.render(grid_dev, "dda", cam, p)
     b, _, _ = ctx.render(grid_host, "dda", cam, p)
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("case", ["blobs", "ct", "random-stddev", "random-chandiff", "leaf-root", "one-voxel"])
+def test_lean_build_renders_like_the_full_build(ctx, case):
+    # XN_BUILD_LEAN writes the device layout directly; everything but svo-rope
+    # must be bit for bit what the full build (node array -> layout) gives
+    import torch
+    import xenodon_gb300 as xg
+    from xenodon_gb300 import volumes
+    heur, thr = "chan-diff", 0
+    if case == "blobs":
+        g = volumes.blobs(64, seed=3)
+    elif case == "ct":
+        g = volumes.ct_shell(80, 57, 80, seed=2, device="cpu")
+    elif case == "random-stddev":
+        g = volumes.random_grid(29, 40, 33, seed=5, density=0.4, levels=6)
+        heur, thr = "std-dev", 9.0
+    elif case == "random-chandiff":
+        g = volumes.random_grid(17, 9, 30, seed=6, density=0.6, levels=8)
+        heur, thr = "chan-diff", 40
+    elif case == "leaf-root":
+        g = np.full((8, 8, 8, 4), 77, np.uint8)
+    else:
+        g = np.full((1, 1, 1, 4), 200, np.uint8)
+    d = torch.from_numpy(np.ascontiguousarray(g)).cuda()
+    dims = (g.shape[2], g.shape[1], g.shape[0])
+    lean, st = ctx.build_svo_volume(d.data_ptr(), dims, "sparse", heur, thr, lean=True)
+    full, st_full = ctx.build_svo_volume(d.data_ptr(), dims, "sparse", heur, thr)
+    assert st == st_full
+    ref, rst = oracle.build_svo(g, "sparse", heur, thr)
+    assert st == rst
+    n_internal = int(np.sum(ref[:, 9] < 0x80000000))
+    if n_internal:
+        assert lean.info()["device_bytes"] == n_internal * 36
+    cams = [((0.3, -0.1, -0.95), (0, 1, -0.105), (0.2, 0.7, 2.2)), ((0.6, 0.3, 0.74), (-0.2, 0.95, 0.0), (0.45, 0.55, 0.5))]
+    p = xg.make_params(67, 45, 10.0)
+    for cam in cams:
+        c = xg.make_camera(*cam)
+        for t in ("svo-naive", "esvo", "svo-df"):
+            a, ea, _ = ctx.render(lean, t, c, p, emission=True)
+            b, eb, _ = ctx.render(full, t, c, p, emission=True)
+            assert np.array_equal(a, b) and np.array_equal(ea, eb), (case, t)
+    if n_internal:
+        with pytest.raises(xg.XenodonError) as e:
+            ctx.render(lean, "svo-rope", xg.make_camera(*cams[0]), p)
+        assert e.value.code == xg.XN_ERR_ARG
+
+
+def test_lean_build_rejects_non_sparse_types(ctx):
+    import torch
+    import xenodon_gb300 as xg
+    d = torch.zeros((4, 4, 4, 4), dtype=torch.uint8, device="cuda")
+    for t in ("rope", "dag"):
+        with pytest.raises(xg.XenodonError) as e:
+            ctx.build_svo_volume(d.data_ptr(), (4, 4, 4), t, lean=True)
+        assert e.value.code == xg.XN_ERR_ARG

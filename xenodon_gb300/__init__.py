@@ -21,6 +21,7 @@ CLI_PATH = PKG / "bin" / "xenodon"
 TRAVERSALS = {"dda": 0, "svo-naive": 1, "esvo": 2, "svo-df": 3, "svo-rope": 4}
 SVO_TRAVERSALS = ("svo-naive", "esvo", "svo-df", "svo-rope")
 SVO_TYPES = {"sparse": 0, "dag": 1, "rope": 2}
+XN_BUILD_LEAN = 0x100  # xn_build_svo_volume: write the device layout directly (sparse trees)
 HEURISTICS = {"chan-diff": 0, "std-dev": 1}
 
 XN_OK = 0
@@ -260,11 +261,16 @@ class Context:
         _check(self.lib.xn_volume_upload_grid_device(self.handle, d_rgba, dims[0], dims[1], dims[2], ctypes.byref(h)))
         return Volume(self, h)
 
-    def build_svo_volume(self, d_rgba: int, dims, svo_type="rope", heuristic="chan-diff", threshold=0.0):
-        """Octree of a device grid, built and kept on the device.  Returns (Volume, stats)."""
+    def build_svo_volume(self, d_rgba: int, dims, svo_type="rope", heuristic="chan-diff", threshold=0.0,
+                         lean: bool = False):
+        """Octree of a device grid, built and kept on the device.  Returns (Volume, stats).
+
+        lean (sparse trees): write the device layout directly, without the
+        reference node array or rope records (every traversal but svo-rope)."""
         h = ctypes.c_void_p()
         st = BuildStats()
-        _check(self.lib.xn_build_svo_volume(self.handle, d_rgba, dims[0], dims[1], dims[2], SVO_TYPES[svo_type],
+        t = SVO_TYPES[svo_type] | (XN_BUILD_LEAN if lean else 0)
+        _check(self.lib.xn_build_svo_volume(self.handle, d_rgba, dims[0], dims[1], dims[2], t,
                                             HEURISTICS[heuristic], float(threshold), ctypes.byref(h), ctypes.byref(st)))
         return Volume(self, h), {f: int(getattr(st, f)) for f, _ in BuildStats._fields_}
 

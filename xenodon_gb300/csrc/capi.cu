@@ -467,6 +467,8 @@ int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_p
         L.inner_depth = v->inner_depth;
         L.leaves = v->leaves;
         L.depth_consistent = v->depth_consistent;
+        if (traversal == XN_TRAV_SVO_ROPE && v->layout == XN_LAYOUT_COMPACT && !v->rinner)
+            return fail(XN_ERR_ARG, "svo-rope: the octree was built lean, without rope records");
         // svo-df and svo-naive through the ray-pool kernel unless
         // XN_RAY_POOL=0 (same results; the switch keeps the one-ray-per-thread
         // kernels reachable)

@@ -34,6 +34,7 @@
 
 #include "../../include/xenodon.h"
 #include "xn_ctx.h"
+#include "xn_internal.h"
 #include "xn_scan.cuh"
 
 namespace xn {
@@ -97,6 +98,7 @@ struct UpArgs {
     double stddev;          // StdDev threshold
     unsigned int* ambig_count;
     unsigned long long* ambig_list;
+    int lean;               // subtree sizes count internal nodes only (the lean build)
 };
 
 __device__ __forceinline__ void cell_coords(uint64_t i, const LevelGeom& L, uint32_t& x, uint32_t& y, uint32_t& z) {
@@ -112,7 +114,7 @@ __device__ __forceinline__ uint64_t cell_index(const LevelGeom& L, uint32_t x, u
 
 // Subtree size of child k of an internal cell (x, y, z) of the current level.
 __device__ __forceinline__ uint64_t child_size(const UpArgs& a, uint32_t x, uint32_t y, uint32_t z, int k) {
-    if (a.child_is_voxel) return 1;
+    if (a.child_is_voxel) return a.lean ? 0 : 1;
     uint32_t cx = 2 * x + ((k >> 2) & 1), cy = 2 * y + ((k >> 1) & 1), cz = 2 * z + (k & 1);
     return a.child_size[cell_index(a.child, cx, cy, cz)];
 }
@@ -128,7 +130,7 @@ __global__ void up_level_kernel(UpArgs a) {
     const uint64_t ox = x * e, oy = y * e, oz = z * e;
     const bool inside = ox < a.g.dx && oy < a.g.dy && oz < a.g.dz;
     if (!inside) {  // OctreeConstruction.h:146-154
-        a.size[i] = 1;
+        a.size[i] = a.lean ? 0 : 1;
         a.color[i] = 0;
         a.flags[i] = F_LEAF;
         return;
@@ -217,7 +219,7 @@ __global__ void up_level_kernel(UpArgs a) {
     }
     const bool leaf = (!split && fully) || e == 1;
     a.flags[i] = (leaf ? F_LEAF : 0) | F_INSIDE | (ambiguous ? F_AMBIG : 0);
-    uint64_t sz = 1;
+    uint64_t sz = leaf && a.lean ? 0 : 1;
     if (!leaf) {
 #pragma unroll
         for (int k = 0; k < 8; ++k) sz += child_size(a, x, y, z, k);
@@ -265,7 +267,7 @@ __global__ void resize_level_kernel(UpArgs a) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.cur.n) return;
     if (a.flags[i] & F_LEAF) {
-        a.size[i] = 1;
+        a.size[i] = a.lean ? 0 : 1;
         return;
     }
     uint32_t x, y, z;
@@ -285,6 +287,8 @@ struct DownArgs {
     const unsigned long long* child_size;
     const uint32_t* color;
     const uint8_t* flags;
+    const uint32_t* child_color;  // lean build: the child level's colours and flags
+    const uint8_t* child_flags;
     const unsigned long long* start;
     unsigned long long* child_start;
     uint32_t* nodes;  // n_total x 10 words, or null when only the starts are wanted
@@ -360,6 +364,60 @@ __global__ void down_level_kernel(DownArgs a) {
     if ((threadIdx.x & 31) == 0) {
         if (leaves) atomicAdd(a.leaves, leaves);
         if (exist) atomicAdd(a.existing, exist);
+        if (internal) atomicAdd(a.existing + 1, internal);
+        if (deepest) atomicMax(a.max_depth, deepest);
+    }
+}
+
+// The lean build's top-down pass: sizes and starts count internal nodes only,
+// so index N - start - size is a node's rank among the internal nodes in the
+// reference's node order -- the order the device layout (svo_layout.cu) gives
+// them.  Every internal cell writes its eight child words (leaf: bit 31 | RGB,
+// internal: that child's rank) and its depth; leaves write nothing.
+__global__ void lean_down_kernel(DownArgs a, uint32_t* inner, uint32_t* inner_depth) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long leaves = 0, internal = 0;
+    unsigned int deepest = 0;
+    const uint64_t st = i < a.cur.n ? a.start[i] : NONE;
+    if (st != NONE && !(a.flags[i] & F_LEAF)) {
+        internal = 1;
+        const uint64_t idx = a.n_total - st - a.size[i];
+        uint32_t x, y, z;
+        cell_coords(i, a.cur, x, y, z);
+        uint64_t run = st;
+        uint32_t ch[8];
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t cx = 2 * x + ((k >> 2) & 1), cy = 2 * y + ((k >> 1) & 1), cz = 2 * z + (k & 1);
+            if (a.child_is_voxel) {
+                const uint32_t v = (cx < a.g.dx && cy < a.g.dy && cz < a.g.dz) ? vox_at(a.g, cx, cy, cz) : 0u;
+                ch[k] = LEAF | (v & 0xFFFFFFu);
+                ++leaves;
+            } else {
+                const uint64_t ci = cell_index(a.child, cx, cy, cz);
+                if (a.child_flags[ci] & F_LEAF) {
+                    ch[k] = LEAF | (a.child_color[ci] & 0xFFFFFFu);
+                    ++leaves;
+                } else {
+                    const uint64_t cS = a.child_size[ci];
+                    a.child_start[ci] = run;
+                    ch[k] = (uint32_t)(a.n_total - run - cS);
+                    run += cS;
+                }
+            }
+        }
+        deepest = leaves ? (unsigned)a.depth + 1 : 0;
+        uint4* p = reinterpret_cast<uint4*>(inner + idx * 8);
+        p[0] = make_uint4(ch[0], ch[1], ch[2], ch[3]);
+        p[1] = make_uint4(ch[4], ch[5], ch[6], ch[7]);
+        inner_depth[idx] = (uint32_t)a.depth;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        leaves += __shfl_down_sync(0xFFFFFFFFu, leaves, o);
+        internal += __shfl_down_sync(0xFFFFFFFFu, internal, o);
+        deepest = max(deepest, __shfl_down_sync(0xFFFFFFFFu, deepest, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (leaves) atomicAdd(a.leaves, leaves);
         if (internal) atomicAdd(a.existing + 1, internal);
         if (deepest) atomicMax(a.max_depth, deepest);
     }
@@ -681,7 +739,8 @@ int exclusive_scan(Scratch& sc, const In* in, uint64_t n, unsigned* out, cudaStr
 // device (packed RGBA, x fastest).  On success *d_nodes is a device buffer of
 // n_nodes*10 words owned by the caller through ctx->device_free.
 int build_svo_device(Ctx* c, const uint32_t* d_vox, uint32_t dx, uint32_t dy, uint32_t dz, int type, int heuristic,
-                     double threshold, uint32_t** d_nodes, uint64_t* d_nodes_bytes, xn_build_stats* stats) {
+                     double threshold, uint32_t** d_nodes, uint64_t* d_nodes_bytes, xn_build_stats* stats,
+                     Volume* lean) {
     cudaStream_t s = c->stream;
     const uint64_t side = std::max(ceil_pow2(dx), std::max(ceil_pow2(dy), ceil_pow2(dz)));
     int L = 0;
@@ -692,6 +751,7 @@ int build_svo_device(Ctx* c, const uint32_t* d_vox, uint32_t dx, uint32_t dy, ui
     *d_nodes = nullptr;
     *d_nodes_bytes = 0;
     if (L >= MAX_LEVELS) return fail(XN_ERR_ARG, "xn_build_svo: grid too large");
+    if (lean && L == 0) return LEAN_LEAF_ROOT;
 
     if (L == 0) {  // a single voxel: the root is a depth-0 leaf
         uint32_t* nodes = nullptr;
@@ -744,12 +804,13 @@ int build_svo_device(Ctx* c, const uint32_t* d_vox, uint32_t dx, uint32_t dy, ui
     const uint64_t stat_bytes = heuristic == XN_HEUR_STD_DEV ? sizeof(SDStats) : sizeof(CDStats);
     void* stats_buf[2] = {nullptr, nullptr};
     {
-        uint64_t big = 0;
-        for (int d = 0; d < L; ++d) big = std::max(big, geo[d].n);
+        // level d writes buffer d & 1 and reads d + 1's: size each for its own levels
+        uint64_t big[2] = {1, 1};
+        for (int d = 0; d < L; ++d) big[d & 1] = std::max(big[d & 1], geo[d].n);
         uint8_t* p0 = nullptr;
         uint8_t* p1 = nullptr;
-        if ((r = sc.alloc(&p0, big * stat_bytes, "xn_build_svo: scan statistics")) ||
-            (r = sc.alloc(&p1, big * stat_bytes, "xn_build_svo: scan statistics")))
+        if ((r = sc.alloc(&p0, big[0] * stat_bytes, "xn_build_svo: scan statistics")) ||
+            (r = sc.alloc(&p1, big[1] * stat_bytes, "xn_build_svo: scan statistics")))
             return r;
         stats_buf[0] = p0;
         stats_buf[1] = p1;
@@ -785,6 +846,7 @@ int build_svo_device(Ctx* c, const uint32_t* d_vox, uint32_t dx, uint32_t dy, ui
         a.stddev = threshold;
         a.ambig_count = counters;
         a.ambig_list = ambig_list;
+        a.lean = lean ? 1 : 0;
         if (heuristic == XN_HEUR_STD_DEV) {
             if ((e = cudaMemsetAsync(counters, 0, 4, s)) != cudaSuccess) break;
             up_level_kernel<XN_HEUR_STD_DEV><<<blocks_for(geo[d].n, T), T, 0, s>>>(a);
@@ -817,6 +879,70 @@ int build_svo_device(Ctx* c, const uint32_t* d_vox, uint32_t dx, uint32_t dy, ui
     if ((e = cudaMemcpyAsync(&n_total, size[0], 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess)
         return cuda_fail(e, "xn_build_svo");
+    if (lean) {
+        if (n_total == 0) return LEAN_LEAF_ROOT;
+        if (n_total >= LEAF) return fail(XN_ERR_FORMAT, "xn_build_svo: more than 2^31 internal nodes");
+        // ---- top-down, lean: the device layout's inner nodes only
+        lean->n_inner = n_total;
+        lean->n_leaves = 0;
+        if ((r = c->device_alloc(reinterpret_cast<void**>(&lean->inner), n_total * 32, "xn_build_svo: inner nodes")) ||
+            (r = c->device_alloc(reinterpret_cast<void**>(&lean->inner_depth), n_total * 4,
+                                 "xn_build_svo: inner depths"))) {
+            lean->release_layout();
+            return r;
+        }
+        for (int d = 0; d < L && e == cudaSuccess; ++d) e = cudaMemsetAsync(start[d], 0xFF, geo[d].n * 8, s);
+        const unsigned long long zero = 0;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(start[0], &zero, 8, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, 16, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(leaf_count, 0, 8, s);
+        unsigned long long* counts = nullptr;  // [1]: internal nodes written
+        if ((r = sc.alloc(&counts, 2, "xn_build_svo: counters"))) {
+            lean->release_layout();
+            return r;
+        }
+        if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, 16, s);
+        for (int d = 0; d < L && e == cudaSuccess; ++d) {
+            DownArgs a{};
+            a.g = g;
+            a.cur = geo[d];
+            a.child_is_voxel = d == L - 1;
+            if (d < L - 1) a.child = geo[d + 1];
+            a.depth = d;
+            a.n_total = n_total;
+            a.size = size[d];
+            a.child_size = d < L - 1 ? size[d + 1] : nullptr;
+            a.flags = flags[d];
+            a.child_color = d < L - 1 ? color[d + 1] : nullptr;
+            a.child_flags = d < L - 1 ? flags[d + 1] : nullptr;
+            a.start = start[d];
+            a.child_start = d < L - 1 ? start[d + 1] : nullptr;
+            a.leaves = leaf_count;
+            a.max_depth = counters + 1;
+            a.existing = counts;
+            lean_down_kernel<<<blocks_for(geo[d].n, T), T, 0, s>>>(a, lean->inner, lean->inner_depth);
+            e = cudaGetLastError();
+        }
+        unsigned long long leaves = 0, hcounts[2] = {0, 0};
+        unsigned int hc[2] = {0, 0};
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&leaves, leaf_count, 8, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hc, counters, 8, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hcounts, counts, 16, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e == cudaSuccess && hcounts[1] != n_total) {
+            lean->release_layout();
+            return fail(XN_ERR_STATE, "xn_build_svo: %llu of %llu internal nodes written",
+                        (unsigned long long)hcounts[1], (unsigned long long)n_total);
+        }
+        if (e != cudaSuccess) {
+            lean->release_layout();
+            return cuda_fail(e, "xn_build_svo: top-down pass");
+        }
+        stats->total_leaves = stats->unique_leaves = leaves;
+        stats->total_nodes = stats->n_nodes = n_total + leaves;
+        stats->depth = hc[1];
+        return XN_OK;
+    }
     if (n_total > 0xFFFFFFFFull)
         return fail(XN_ERR_FORMAT, "xn_build_svo: %llu nodes exceed the 32-bit node indices of the SVO format",
                     (unsigned long long)n_total);
@@ -1039,8 +1165,12 @@ XN_API int xn_build_svo_volume(xn_ctx* h, const void* d_rgba, uint32_t dx, uint3
     if (!h || !d_rgba || !out || !stats) return fail(XN_ERR_ARG, "xn_build_svo_volume: NULL argument");
     *out = nullptr;
     if (!dx || !dy || !dz) return fail(XN_ERR_ARG, "xn_build_svo_volume: empty grid %ux%ux%u", dx, dy, dz);
+    const bool lean = (type & XN_BUILD_LEAN) != 0;
+    type &= ~XN_BUILD_LEAN;
     if (type < XN_SVO_SPARSE || type > XN_SVO_ROPE_TREE)
         return fail(XN_ERR_ARG, "xn_build_svo_volume: invalid type %d", type);
+    if (lean && type != XN_SVO_SPARSE)
+        return fail(XN_ERR_ARG, "xn_build_svo_volume: XN_BUILD_LEAN builds sparse trees only");
     if (heuristic == XN_HEUR_CHANNEL_DIFF) {
         if (!(threshold >= 0.0 && threshold <= 255.0) || threshold != (double)(int)threshold)
             return fail(XN_ERR_ARG, "xn_build_svo_volume: --chan-diff must be an integer in 0..255");
@@ -1055,6 +1185,28 @@ XN_API int xn_build_svo_volume(xn_ctx* h, const void* d_rgba, uint32_t dx, uint3
     if (r) return r;
     uint32_t* d_nodes = nullptr;
     uint64_t nbytes = 0;
+    if (lean) {
+        // straight into the device layout: no reference nodes, no rope records
+        Volume* v = new (std::nothrow) Volume();
+        if (!v) return fail(XN_ERR_NOMEM, "xn_build_svo_volume: out of host memory");
+        v->ctx = c;
+        r = build_svo_device(c, static_cast<const uint32_t*>(d_rgba), dx, dy, dz, type, heuristic, threshold,
+                             &d_nodes, &nbytes, stats, v);
+        if (r == XN_OK) {
+            v->kind = XN_VOLUME_SVO;
+            v->side = stats->side;
+            v->n_nodes = stats->n_nodes;
+            const uint64_t sd = stats->side > 0xFFFFFFFFull ? 0xFFFFFFFFull : stats->side;
+            v->dim[0] = v->dim[1] = v->dim[2] = (uint32_t)sd;
+            v->layout = XN_LAYOUT_COMPACT;
+            v->depth_consistent = 1;  // written from the tree itself
+            *out = reinterpret_cast<xn_volume*>(v);
+            return XN_OK;
+        }
+        delete v;
+        if (r != LEAN_LEAF_ROOT) return r;
+        // the root is a leaf: the one-node tree keeps the reference layout
+    }
     r = build_svo_device(c, static_cast<const uint32_t*>(d_rgba), dx, dy, dz, type, heuristic, threshold, &d_nodes,
                          &nbytes, stats);
     if (r) return r;

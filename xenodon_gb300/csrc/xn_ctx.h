@@ -68,7 +68,10 @@ struct Volume {
     uint32_t* leaves = nullptr;
     int depth_consistent = 0;  // internal nodes' depth fields match the tree (svo_layout.cu)
 
-    uint64_t layout_bytes() const { return n_inner * 68 + n_leaves * 32; }
+    uint64_t layout_bytes() const {
+        return (inner ? n_inner * 32 : 0) + (rinner ? n_inner * 32 : 0) + (inner_depth ? n_inner * 4 : 0) +
+               (leaves ? n_leaves * 32 : 0);
+    }
     void release_layout() {
         if (!ctx) return;
         ctx->device_free(inner, n_inner * 32);
@@ -80,6 +83,15 @@ struct Volume {
 };
 
 int build_svo_layout(Ctx* c, Volume* v);
+
+// Octree build on the device (svo_build.cu).  With lean == nullptr: the
+// reference node array in *d_nodes.  With lean: only the device layout's
+// inner / inner_depth arrays, written into *lean (sparse trees; no rope
+// records); returns LEAN_LEAF_ROOT when the root is a leaf (no internal nodes).
+constexpr int LEAN_LEAF_ROOT = 1;
+int build_svo_device(Ctx* c, const uint32_t* d_vox, uint32_t dx, uint32_t dy, uint32_t dz, int type, int heuristic,
+                     double threshold, uint32_t** d_nodes, uint64_t* d_nodes_bytes, xn_build_stats* stats,
+                     Volume* lean = nullptr);
 
 int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
 int cuda_fail(cudaError_t e, const char* what);
