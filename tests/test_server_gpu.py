@@ -75,9 +75,13 @@ def test_results_equal_alone_and_in_the_mix(ctx, volumes_data):
 def test_lru_eviction_under_a_tight_budget(ctx, volumes_data):
     import xenodon_gb300 as xg
     # room for the largest volume plus frames, not for all four volumes
-    sizes = {vid: (d.nbytes if k == "grid" else d[0].shape[0] * 72) for vid, (k, d) in volumes_data.items()}
-    budget = max(sizes.values()) + 4 * 120 * 64 * 4 + (1 << 20)
-    assert budget < sum(sizes.values())
+    alone = {vid: (ctx.upload_grid(d) if k == "grid" else ctx.upload_svo(d[0], d[1]))
+             for vid, (k, d) in volumes_data.items()}
+    sizes = {vid: v.info()["device_bytes"] for vid, v in alone.items()}
+    for v in alone.values():
+        v.release()
+    budget = max(sizes.values()) + 4 * 120 * 64 * 4 + (64 << 10)
+    assert budget < sum(sizes.values()) - min(sizes.values())
     rng = np.random.default_rng(5)
     with xg.Server(ctx, hbm_budget=budget, max_batch_jobs=4, streams=1) as server:
         vols = _register(server, ctx, volumes_data)

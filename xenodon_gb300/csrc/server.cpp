@@ -369,7 +369,11 @@ XN_API int xn_server_add_svo(xn_server* s, uint32_t id, const uint32_t* nodes, u
     v.kind = XN_VOLUME_SVO;
     v.nodes.assign(nodes, nodes + n * 10);
     v.side = side;
-    v.estimate = n * 40 + n * 8;  // reference nodes during upload plus the device layout
+    // the resident size of the device layout (svo_layout.cu): 68 bytes per
+    // internal node and 32 per leaf; a leaf root keeps the 40-byte node
+    uint64_t n_inner = 0;
+    for (uint64_t i = 0; i < n; ++i) n_inner += nodes[i * 10 + 9] < 0x80000000u ? 1 : 0;
+    v.estimate = n_inner ? n_inner * 68 + (n - n_inner) * 32 : n * 40;
     return XN_OK;
 }
 
