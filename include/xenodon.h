@@ -255,8 +255,8 @@ XN_API void xn_free(void* p);
 
 /* `xenodon convert` followed by an upload, without leaving the device: builds
  * the octree of a grid in device memory (d_rgba: packed RGBA8 texels, x
- * fastest) and makes it a resident volume.  The node array is the one
- * xn_build_svo returns.
+ * fastest; a host pointer is copied to the device first) and makes it a
+ * resident volume.  The node array is the one xn_build_svo returns.
  *
  * type | XN_BUILD_LEAN (sparse trees only) writes the device layout directly
  * and never holds the 40-byte node array: about 36 bytes per internal node
@@ -295,6 +295,15 @@ XN_API int xn_build_svo_static(const uint32_t* d_rgba, uint32_t dx, uint32_t dy,
  * side, u64 node count, nodes of 10 LE u32.  load returns malloc'd nodes. */
 XN_API int xn_svo_load(const char* path, uint32_t** nodes_out, uint64_t* n_nodes, uint64_t* side);
 XN_API int xn_svo_save(const char* path, const uint32_t* nodes, uint64_t n_nodes, uint64_t side);
+
+/* The format extension for octrees the reference's format cannot hold (2^32
+ * nodes or more; no counterpart in the reference): a resident octree volume's
+ * device layout written to disk ("XNDN-SVC", versioned; internal nodes only,
+ * 36 bytes each, plus the rope records when the volume has them) and read
+ * back straight into HBM.  Both stream through pinned chunks; load validates
+ * every index on the device before the volume can be rendered. */
+XN_API int xn_volume_save(xn_ctx* ctx, const xn_volume* volume, const char* path);
+XN_API int xn_volume_load(xn_ctx* ctx, const char* path, xn_volume** out);
 
 /* Grid::load_tiff (src/model/Grid.cpp:27-79): a stacked TIFF, one page per z
  * slice, read the way TIFFReadRGBAImage hands it to the reference (rows

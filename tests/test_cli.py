@@ -86,6 +86,8 @@ def test_missing_config_file(conf):
     (("--chan-diff", "256", "a.tif", "b.svo"), "Invalid value for <channel difference> of parameter --chan-diff"),
     (("--std-dev", "-1", "a.tif", "b.svo"), "Invalid value for <std. dev> of parameter --std-dev"),
     (("a.tif",), "Missing required positional argument <destination svo path>"),
+    (("--lean", "a.tif", "b.svo"), "--lean builds a sparse tree into a .svc file (no --dag or --rope)"),
+    (("--lean", "--rope", "a.tif", "b.svc"), "--lean builds a sparse tree into a .svc file (no --dag or --rope)"),
 ])
 def test_convert_argument_errors(conf, args, msg):
     rc, out = run("convert", *args, cwd=conf)

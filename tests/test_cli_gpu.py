@@ -147,3 +147,28 @@ def test_camera_script_errors(ctx, tmp_path):
     assert rc == 1 and "Error: Syntax error in camera input file" in out
     rc, out = run("render", "--headless", "h.conf", "v.tif", "--camera", "none.txt", "-q", cwd=tmp_path)
     assert rc == 1 and "Error: Failed to open 'none.txt'" in out
+
+
+@pytest.mark.parametrize("flags,shaders", [(["--rope"], ["svo-rope", "esvo"]), (["--lean"], ["svo-df", "svo-naive"])])
+def test_convert_to_device_layout_file_and_render_it(ctx, tmp_path, flags, shaders):
+    # .svc destinations hold the device layout; rendering them gives the
+    # frames of the same tree converted to .svo
+    import xenodon_gb300 as xg
+    from xenodon_gb300 import volumes
+    g = volumes.blobs(32, seed=9)
+    xg.tiff_save(tmp_path / "v.tif", g)
+    rc, out = run("convert", *[f for f in flags if f != "--lean"], "v.tif", "v.svo", cwd=tmp_path)
+    assert rc == 0, out
+    rc, out_svc = run("convert", *flags, "v.tif", "v.svc", cwd=tmp_path)
+    assert rc == 0, out_svc
+    # the same build report (stats of the same tree)
+    assert out.split("Generated octree:")[1] == out_svc.split("Generated octree:")[1]
+    (tmp_path / "h.conf").write_text("device {\n vkindex = 0\n offset = (0, 0)\n extent = (40, 30)\n}\n")
+    _write_cams(tmp_path / "cam.txt")
+    for sh in shaders:
+        for vol, pat in (("v.svo", "a-{}.png"), ("v.svc", "b-{}.png")):
+            rc, o = run("render", "--headless", "h.conf", vol, "-s", sh, "--camera", "cam.txt", "-e", "10",
+                        "--output", pat, cwd=tmp_path)
+            assert rc == 0, o
+        for i in range(len(CAMS)):
+            assert np.array_equal(png_pixels(tmp_path / f"a-{i}.png"), png_pixels(tmp_path / f"b-{i}.png")), sh

@@ -36,7 +36,8 @@ EXPORTS = (
     "xn_render_batch", "xn_autotune_batch", "xn_batch_graph_create", "xn_batch_graph_launch",
     "xn_batch_graph_destroy", "xn_server_create", "xn_server_destroy", "xn_server_add_grid",
     "xn_server_add_svo", "xn_server_submit", "xn_server_wait", "xn_server_stats",
-    "xn_svo_load", "xn_svo_save", "xn_tiff_load", "xn_tiff_save", "xn_png_save",
+    "xn_svo_load", "xn_svo_save", "xn_volume_save", "xn_volume_load", "xn_tiff_load", "xn_tiff_save",
+    "xn_png_save",
 )
 
 
@@ -145,6 +146,8 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "xn_server_stats": (i32, [vp, P(ServerStats)]),
         "xn_svo_load": (i32, [ctypes.c_char_p, P(P(u32)), P(u64), P(u64)]),
         "xn_svo_save": (i32, [ctypes.c_char_p, vp, u64, u64]),
+        "xn_volume_save": (i32, [vp, vp, ctypes.c_char_p]),
+        "xn_volume_load": (i32, [vp, ctypes.c_char_p, ctypes.POINTER(vp)]),
         "xn_tiff_load": (i32, [ctypes.c_char_p, P(P(ctypes.c_uint8)), P(u32 * 3)]),
         "xn_tiff_save": (i32, [ctypes.c_char_p, vp, u32, u32, u32]),
         "xn_png_save": (i32, [ctypes.c_char_p, vp, u32, u32]),
@@ -200,6 +203,10 @@ class Volume:
         _check(load_library().xn_volume_info_get(self.handle, ctypes.byref(vi)))
         return {"kind": "grid" if vi.kind == 0 else "svo", "dim": tuple(vi.dim), "side": vi.side,
                 "n_nodes": vi.n_nodes, "device_bytes": vi.device_bytes, "has_ropes": bool(vi.has_ropes)}
+
+    def save(self, path) -> None:
+        """Write an octree volume's device layout ("XNDN-SVC"; xn_volume_save)."""
+        _check(load_library().xn_volume_save(self.ctx.handle, self.handle, str(path).encode()))
 
     def release(self) -> None:
         if self.handle:
@@ -273,6 +280,12 @@ class Context:
         _check(self.lib.xn_build_svo_volume(self.handle, d_rgba, dims[0], dims[1], dims[2], t,
                                             HEURISTICS[heuristic], float(threshold), ctypes.byref(h), ctypes.byref(st)))
         return Volume(self, h), {f: int(getattr(st, f)) for f, _ in BuildStats._fields_}
+
+    def load_volume(self, path) -> Volume:
+        """Read an "XNDN-SVC" octree volume file straight into HBM (xn_volume_load)."""
+        h = ctypes.c_void_p()
+        _check(self.lib.xn_volume_load(self.handle, str(path).encode(), ctypes.byref(h)))
+        return Volume(self, h)
 
     def upload_svo(self, nodes: np.ndarray, side: int) -> Volume:
         """nodes: uint32 (n, 10) in the reference layout."""

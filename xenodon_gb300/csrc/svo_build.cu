@@ -1183,6 +1183,32 @@ XN_API int xn_build_svo_volume(xn_ctx* h, const void* d_rgba, uint32_t dx, uint3
     std::lock_guard<std::mutex> lk(c->mu);
     int r = c->activate();
     if (r) return r;
+    // a grid in host memory is copied to the device for the build
+    cudaPointerAttributes pa{};
+    const uint32_t* d_vox = static_cast<const uint32_t*>(d_rgba);
+    void* staged = nullptr;
+    const uint64_t grid_bytes = (uint64_t)dx * dy * dz * 4;
+    if (cudaPointerGetAttributes(&pa, d_rgba) != cudaSuccess) cudaGetLastError();
+    if (pa.type != cudaMemoryTypeDevice && pa.type != cudaMemoryTypeManaged) {
+        if ((r = c->device_alloc(&staged, grid_bytes, "xn_build_svo_volume: grid"))) return r;
+        cudaError_t e = cudaMemcpyAsync(staged, d_rgba, grid_bytes, cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) {
+            c->device_free(staged, grid_bytes);
+            return cuda_fail(e, "xn_build_svo_volume: grid upload");
+        }
+        d_vox = static_cast<const uint32_t*>(staged);
+    }
+    struct Staged {
+        Ctx* c;
+        void* p;
+        uint64_t bytes;
+        ~Staged() {
+            if (p) {
+                cudaStreamSynchronize(c->stream);
+                c->device_free(p, bytes);
+            }
+        }
+    } staged_guard{c, staged, grid_bytes};
     uint32_t* d_nodes = nullptr;
     uint64_t nbytes = 0;
     if (lean) {
@@ -1190,8 +1216,7 @@ XN_API int xn_build_svo_volume(xn_ctx* h, const void* d_rgba, uint32_t dx, uint3
         Volume* v = new (std::nothrow) Volume();
         if (!v) return fail(XN_ERR_NOMEM, "xn_build_svo_volume: out of host memory");
         v->ctx = c;
-        r = build_svo_device(c, static_cast<const uint32_t*>(d_rgba), dx, dy, dz, type, heuristic, threshold,
-                             &d_nodes, &nbytes, stats, v);
+        r = build_svo_device(c, d_vox, dx, dy, dz, type, heuristic, threshold, &d_nodes, &nbytes, stats, v);
         if (r == XN_OK) {
             v->kind = XN_VOLUME_SVO;
             v->side = stats->side;
@@ -1207,8 +1232,7 @@ XN_API int xn_build_svo_volume(xn_ctx* h, const void* d_rgba, uint32_t dx, uint3
         if (r != LEAN_LEAF_ROOT) return r;
         // the root is a leaf: the one-node tree keeps the reference layout
     }
-    r = build_svo_device(c, static_cast<const uint32_t*>(d_rgba), dx, dy, dz, type, heuristic, threshold, &d_nodes,
-                         &nbytes, stats);
+    r = build_svo_device(c, d_vox, dx, dy, dz, type, heuristic, threshold, &d_nodes, &nbytes, stats);
     if (r) return r;
     Volume* v = new (std::nothrow) Volume();
     if (!v) {

@@ -42,8 +42,8 @@ const char* HELP_RENDER =
     "Usage: xenodon render --headless <config> [options] <volume>\n"
     "\n"
     "Renders <volume> frame by frame and writes each frame to a PNG file.\n"
-    "The volume type follows the extension (.tif/.tiff: grid, .svo: octree)\n"
-    "unless --volume-type says otherwise.\n"
+    "The volume type follows the extension (.tif/.tiff: grid, .svo: octree,\n"
+    ".svc: octree in the device layout) unless --volume-type says otherwise.\n"
     "\n"
     "Options:\n"
     "  --headless <config>     Region layout, see 'xenodon help headless-config'.\n"
@@ -59,14 +59,16 @@ const char* HELP_RENDER =
     "                          e.g. 'out-{:0>3}.png' (default 'out-{}.png').\n"
     "  --discard-output        Write no images (for benchmarking).\n"
     "  --stats-output <file>   Per-frame timing statistics.\n"
-    "  --volume-type <type>    tiff, tif or svo.\n"
+    "  --volume-type <type>    tiff, tif, svo or svc.\n"
     "  --log-output <file>     Copy of the log.\n"
     "  -q, --quiet             No log on standard output.\n";
 
 const char* HELP_CONVERT =
     "Usage: xenodon convert [options] <source tiff> <destination svo>\n"
     "\n"
-    "Builds a sparse voxel octree from a stacked TIFF on the GPU.\n"
+    "Builds a sparse voxel octree from a stacked TIFF on the GPU.  A destination\n"
+    "ending in .svc receives the device layout (internal nodes only; no 2^32\n"
+    "node limit) instead of the XNDN-SVO node array.\n"
     "\n"
     "Options:\n"
     "  --dag             Merge identical subtrees into a directed acyclic graph.\n"
@@ -74,7 +76,9 @@ const char* HELP_CONVERT =
     "  --chan-diff <n>   Merge a region into one leaf when no colour channel\n"
     "                    varies by more than n (0-255; 0 is lossless).\n"
     "  --std-dev <x>     Merge a region when the standard deviation of its\n"
-    "                    colours is at most x.\n";
+    "                    colours is at most x.\n"
+    "  --lean            (.svc, sparse trees) Build straight into the device\n"
+    "                    layout, never holding the node array; not for svo-rope.\n";
 
 const char* HELP_HEADLESS =
     "The headless configuration lists the output regions:\n"
@@ -115,16 +119,17 @@ std::string lower_ext(const std::string& path) {
     return path.substr(dot + 1);
 }
 
-enum class FileType { Tiff, Svo, Unknown };
+enum class FileType { Tiff, Svo, Svc, Unknown };
 
 FileType parse_file_type(const std::string& s) {
     if (s == "tiff" || s == "tif") return FileType::Tiff;
     if (s == "svo") return FileType::Svo;
+    if (s == "svc") return FileType::Svc;  // device-layout octree file (xn_volume_save)
     return FileType::Unknown;
 }
 
 const char* file_type_name(FileType t) {
-    return t == FileType::Tiff ? "tiff" : t == FileType::Svo ? "svo" : "unknown";
+    return t == FileType::Tiff ? "tiff" : t == FileType::Svo ? "svo" : t == FileType::Svc ? "svc" : "unknown";
 }
 
 struct ShaderOption {
@@ -290,12 +295,12 @@ int render(const std::vector<std::string>& args) {
             for (const auto& s : SHADERS)
                 if (o.shader == s.name) shader = &s;
             if (!shader) throw cli::Error("Invalid shader '" + o.shader + "'");
-            if (shader->type != type)
+            if (shader->type != (type == FileType::Svc ? FileType::Svo : type))
                 throw cli::Error("Shader '" + o.shader + "' is incompatible with model type '" + file_type_name(type) +
                                  "' (requires '" + file_type_name(shader->type) + "')");
         } else {
             for (const auto& s : SHADERS)
-                if (s.type == type) { shader = &s; break; }
+                if (s.type == (type == FileType::Svc ? FileType::Svo : type)) { shader = &s; break; }
         }
         log.log(std::string("Using shader '") + shader->name + "'");
 
@@ -308,6 +313,11 @@ int render(const std::vector<std::string>& args) {
             int r = xn_volume_upload_grid(ctx, rgba, dim[0], dim[1], dim[2], &vol);
             xn_free(rgba);
             check(r);
+        } else if (type == FileType::Svc) {
+            if (xn_volume_load(ctx, o.volume.c_str(), &vol) != XN_OK) throw cli::Error(xn_last_error());
+            xn_volume_info info{};
+            check(xn_volume_info_get(vol, &info));
+            dim[0] = dim[1] = dim[2] = (uint32_t)info.side;
         } else {
             uint32_t* nodes = nullptr;
             uint64_t n = 0, side = 0;
@@ -439,11 +449,11 @@ int render(const std::vector<std::string>& args) {
 
 int convert(const std::vector<std::string>& args) {
     std::string src, dst;
-    bool dag = false, rope = false;
+    bool dag = false, rope = false, lean = false;
     int64_t chan = -1;
     double sd = -1;
     cli::Command cmd;
-    cmd.flags = {{&dag, "--dag"}, {&rope, "--rope"}};
+    cmd.flags = {{&dag, "--dag"}, {&rope, "--rope"}, {&lean, "--lean"}};
     cmd.parameters = {
         {[&](const std::string& a) {
              uint64_t v;
@@ -474,6 +484,13 @@ int convert(const std::vector<std::string>& args) {
         std::printf("Error: --std-dev and --chan-diff are mutually exclusive\n");
         return 1;
     }
+    // a .svc destination gets the device layout (xn_volume_save), built on
+    // the device and written from it; --lean never forms the node array
+    const bool svc = lower_ext(dst) == "svc";
+    if (lean && (!svc || dag || rope)) {
+        std::printf("Error: --lean builds a sparse tree into a .svc file (no --dag or --rope)\n");
+        return 1;
+    }
     std::printf("Loading source...\n");
     uint8_t* rgba = nullptr;
     uint32_t dim[3];
@@ -490,13 +507,16 @@ int convert(const std::vector<std::string>& args) {
     std::fflush(stdout);
     xn_ctx* ctx = nullptr;
     uint32_t* nodes = nullptr;
+    xn_volume* vol = nullptr;
     xn_build_stats st{};
     int r = xn_create(0, 0, &ctx);
     if (r == XN_OK) {
         const int type = dag ? XN_SVO_DAG : rope ? XN_SVO_ROPE_TREE : XN_SVO_SPARSE;
-        r = sd >= 0 ? xn_build_svo(ctx, rgba, dim[0], dim[1], dim[2], type, XN_HEUR_STD_DEV, sd, &nodes, &st)
-                    : xn_build_svo(ctx, rgba, dim[0], dim[1], dim[2], type, XN_HEUR_CHANNEL_DIFF,
-                                   (double)std::max<int64_t>(chan, 0), &nodes, &st);
+        const int heur = sd >= 0 ? XN_HEUR_STD_DEV : XN_HEUR_CHANNEL_DIFF;
+        const double thr = sd >= 0 ? sd : (double)std::max<int64_t>(chan, 0);
+        r = svc ? xn_build_svo_volume(ctx, rgba, dim[0], dim[1], dim[2], type | (lean ? XN_BUILD_LEAN : 0), heur, thr,
+                                      &vol, &st)
+                : xn_build_svo(ctx, rgba, dim[0], dim[1], dim[2], type, heur, thr, &nodes, &st);
     }
     xn_free(rgba);
     if (r != XN_OK) {
@@ -523,11 +543,12 @@ int convert(const std::vector<std::string>& args) {
     std::printf(" Unique leaves: %llu\n", (unsigned long long)st.unique_leaves);
     std::printf(" Depth: %llu\n", (unsigned long long)st.depth);
     int rc = 0;
-    if (xn_svo_save(dst.c_str(), nodes, st.n_nodes, st.side) != XN_OK) {
+    if ((svc ? xn_volume_save(ctx, vol, dst.c_str()) : xn_svo_save(dst.c_str(), nodes, st.n_nodes, st.side)) != XN_OK) {
         std::printf("Error writing '%s': %s\n", dst.c_str(), xn_last_error());
         rc = 1;
     }
     xn_free(nodes);
+    xn_volume_release(vol);
     xn_destroy(ctx);
     return rc;
 }
