@@ -298,3 +298,20 @@ def test_ray_pool_equals_one_ray_per_thread(ctx, blob_volumes, monkeypatch, trav
         monkeypatch.delenv("XN_RAY_POOL")
         assert np.array_equal(pooled, plain), cam
         assert np.array_equal(em_pool, em_plain) and np.array_equal(loads_pool, loads_plain), cam
+
+
+@pytest.mark.parametrize("cam", ["oblique", "inside", "grazing"])
+def test_esvo_stack_in_shared_memory_equals_local(ctx, blob_volumes, monkeypatch, cam):
+    # esvo keeps its stack in shared memory by default; XN_ESVO_STACK=local
+    # selects the local-memory form: same bits, same word counts
+    import xenodon_gb300 as xg
+    _, nodes, side = blob_volumes
+    vol = ctx.upload_svo(nodes, side)
+    p, v = _params_pair(xg, 83, 61)
+    shared, _ = check_parity(ctx, "esvo", CAMS[cam], p, v, nodes=nodes, vol=vol, label=f"esvo-shared/{cam}")
+    _, em_s, loads_s = _gpu_counts(ctx, vol, "esvo", xg.make_camera(*CAMS[cam]), p)
+    monkeypatch.setenv("XN_ESVO_STACK", "local")
+    local, _, _ = ctx.render(vol, "esvo", xg.make_camera(*CAMS[cam]), p)
+    _, em_l, loads_l = _gpu_counts(ctx, vol, "esvo", xg.make_camera(*CAMS[cam]), p)
+    assert np.array_equal(shared, local)
+    assert np.array_equal(em_s, em_l) and np.array_equal(loads_s, loads_l)

@@ -474,6 +474,9 @@ int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_p
         // kernels reachable)
         const char* pool = std::getenv("XN_RAY_POOL");
         L.pool = !(pool && pool[0] == '0');
+        // esvo's stack in shared memory unless XN_ESVO_STACK=local
+        const char* es = std::getenv("XN_ESVO_STACK");
+        L.esvo_shared_stack = !(es && std::strcmp(es, "local") == 0);
     }
     for (int i = 0; i < 3; ++i) L.dim[i] = v->dim[i];
     return XN_OK;

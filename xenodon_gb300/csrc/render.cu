@@ -236,8 +236,12 @@ __device__ __forceinline__ uint32_t find(const Acc& a, V3 pos, V3& base, float& 
 // base and side.  The reference's word reads are still 2 per level + 1.
 constexpr int PATH_CACHE = 32;
 
-struct FindPath {
+// The descent path of the last find: its nodes (an array, in local memory)
+// and the scalars, kept apart so that the scalars can stay in registers.
+struct FindPathNodes {
     uint32_t node[PATH_CACHE];
+};
+struct FindPath {
     int depth = -1;  // depth of the last leaf found, -1: none (or too deep to cache)
     V3 base;         // the last leaf's origin
 };
@@ -247,8 +251,8 @@ __device__ __forceinline__ bool in_capture(float p, float o, float size) {
 }
 
 template <bool COUNT, class Acc>
-__device__ __forceinline__ uint32_t find_cached(const Acc& a, FindPath& path, V3 pos, V3& base, float& side,
-                                                uint32_t& loads, uint32_t& err) {
+__device__ __forceinline__ uint32_t find_cached(const Acc& a, FindPath& path, FindPathNodes& pn, V3 pos, V3& base,
+                                                float& side, uint32_t& loads, uint32_t& err) {
     int level = 0;
     float extent = 1.0f;
     uint32_t index = a.root();
@@ -261,13 +265,13 @@ __device__ __forceinline__ uint32_t find_cached(const Acc& a, FindPath& path, V3
         if (in_capture(pos.x, o.x, size) && in_capture(pos.y, o.y, size) && in_capture(pos.z, o.z, size)) {
             level = j;
             extent = size;
-            index = path.node[j];
+            index = pn.node[j];
             offset = o;
             break;
         }
     }
     for (;; ++level) {
-        if (level < PATH_CACHE) path.node[level] = index;
+        if (level < PATH_CACHE) pn.node[level] = index;
         if (a.is_leaf(index)) {
             base = offset;
             side = extent;
@@ -308,12 +312,13 @@ __device__ V3 trace_naive(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t&
     float t = t_min + MIN_STEP;
     uint32_t iter = 0;
     FindPath path;
+    FindPathNodes pn;
     while (t < t_max) {
         if (++iter > SVO_MAX_ITER) { err |= 1u; break; }
         V3 p = rd * t + ro;
         V3 offset;
         float side;
-        uint32_t node = find_cached<COUNT>(a, path, p, offset, side, loads, err);
+        uint32_t node = find_cached<COUNT>(a, path, pn, p, offset, side, loads, err);
         V3 node_min = offset * rrd - bias;
         V3 node_max = (offset + vs(side)) * rrd - bias;
         float u_min = max_elem(vmin(node_min, node_max));
@@ -332,12 +337,13 @@ __device__ V3 trace_naive(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t&
 // step = one find plus one colour sample); same arithmetic and order.
 template <bool COUNT, class Acc>
 struct NaiveTracer {
+    using Stack = FindPathNodes;
     FindPath path;
     V3 ro, rd, rrd, bias, total;
     float t, t_max;
     uint32_t iter;
 
-    __device__ __forceinline__ bool begin(const Acc&, V3 o, V3 d, uint32_t&) {
+    __device__ __forceinline__ bool begin(const Acc&, V3 o, V3 d, uint32_t&, Stack&) {
         ro = o;
         rd = d;
         rrd = vs(1.0f) / rd;
@@ -354,12 +360,12 @@ struct NaiveTracer {
         return t < t_max;
     }
 
-    __device__ __forceinline__ bool step(const Acc& a, uint32_t& loads, uint32_t& err) {
+    __device__ __forceinline__ bool step(const Acc& a, Stack& pn, uint32_t& loads, uint32_t& err) {
         if (++iter > SVO_MAX_ITER) { err |= 1u; return true; }
         const V3 p = rd * t + ro;
         V3 offset;
         float side;
-        const uint32_t node = find_cached<COUNT>(a, path, p, offset, side, loads, err);
+        const uint32_t node = find_cached<COUNT>(a, path, pn, p, offset, side, loads, err);
         const V3 node_min = offset * rrd - bias;
         const V3 node_max = (offset + vs(side)) * rrd - bias;
         float u_min = max_elem(vmin(node_min, node_max));
@@ -571,15 +577,18 @@ __device__ V3 trace_df_masked(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint3
 // the ray is finished.  Same arithmetic and order as trace_df_masked.
 template <bool COUNT, class Acc>
 struct DfTracer {
-    uint32_t node_stack[STACK_DEPTH];
-    uint32_t state_stack[STACK_DEPTH];
+    // the stacks live apart from the scalar state, which stays in registers
+    struct Stack {
+        uint32_t node[STACK_DEPTH];
+        uint32_t state[STACK_DEPTH];  // remaining hit mask | depth << 8
+    };
     V3 rrd, bias, origin, total;
     float side;
     uint32_t node, depth, mask, iter;
     int sp;
     ChildSlabs slabs;
 
-    __device__ __forceinline__ bool begin(const Acc& a, V3 ro, V3 rd, uint32_t& loads) {
+    __device__ __forceinline__ bool begin(const Acc& a, V3 ro, V3 rd, uint32_t& loads, Stack&) {
         rrd = vs(1.0f) / rd;
         bias = rrd * ro;
         origin = vs(0.0f);
@@ -595,13 +604,13 @@ struct DfTracer {
         return true;
     }
 
-    __device__ __forceinline__ bool step(const Acc& a, uint32_t& loads, uint32_t& err) {
+    __device__ __forceinline__ bool step(const Acc& a, Stack& stk, uint32_t& loads, uint32_t& err) {
         if (++iter > SVO_MAX_ITER) { err |= 1u; return true; }
         if (mask == 0) {
             --sp;
             if (sp < 0) return true;
-            node = node_stack[sp];
-            const uint32_t st = state_stack[sp];
+            node = stk.node[sp];
+            const uint32_t st = stk.state[sp];
             mask = st & 0xFFu;
             depth = st >> 8;
             if (COUNT) ++loads;
@@ -628,8 +637,8 @@ struct DfTracer {
         }
         if (k != 7) {
             if (sp >= STACK_DEPTH) { err |= 2u; return true; }
-            node_stack[sp] = node;
-            state_stack[sp] = mask | (depth << 8);
+            stk.node[sp] = node;
+            stk.state[sp] = mask | (depth << 8);
             ++sp;
         }
         origin = v3(origin.x + ((k & 4u) ? side : 0.0f), origin.y + ((k & 2u) ? side : 0.0f),
@@ -651,13 +660,30 @@ __device__ __forceinline__ uint32_t cxor(uint32_t x, bool ax, bool ay, bool az) 
 }
 
 // resources/esvo.comp:30-136
-template <bool COUNT, class Acc>
-__device__ V3 trace_esvo(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& err) {
+// ESVO's (parent, t_max) stack, indexed by scale: in local memory, or in
+// shared memory with one column per thread (entry i of thread t at
+// i * BLOCK_THREADS + t, so a warp touching one scale hits 32 banks).
+struct EsvoLocalStack {
+    uint32_t node[STACK_DEPTH];
+    float tmax[STACK_DEPTH];
+    __device__ __forceinline__ uint32_t& n(uint32_t i) { return node[i]; }
+    __device__ __forceinline__ float& t(uint32_t i) { return tmax[i]; }
+};
+
+struct EsvoSharedStack {
+    uint32_t* node;  // this thread's column
+    float* tmax;
+    __device__ __forceinline__ uint32_t& n(uint32_t i);
+    __device__ __forceinline__ float& t(uint32_t i);
+};
+
+template <bool COUNT, class Acc, class Stack = EsvoLocalStack>
+__device__ V3 trace_esvo(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& err, Stack* shared_stack = nullptr) {
     const uint32_t depth = STACK_DEPTH;
-    uint32_t node_stack[STACK_DEPTH];
-    float t_max_stack[STACK_DEPTH];
+    Stack local;
+    Stack& stk = shared_stack ? *shared_stack : local;
 #pragma unroll
-    for (int i = 0; i < STACK_DEPTH; ++i) { node_stack[i] = 0; t_max_stack[i] = 0.0f; }
+    for (int i = 0; i < STACK_DEPTH; ++i) { stk.n(i) = 0; stk.t(i) = 0.0f; }
 
     V3 t_coeff = v3(1.0f / -fabsf(rd.x), 1.0f / -fabsf(rd.y), 1.0f / -fabsf(rd.z));
     V3 t_bias = t_coeff * ro;
@@ -705,8 +731,8 @@ __device__ V3 trace_esvo(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& 
                     total = total + color * (tv_max - t_min);
                 } else {
                     if (tc_max < h) {
-                        node_stack[scale] = parent;
-                        t_max_stack[scale] = t_max;
+                        stk.n(scale) = parent;
+                        stk.t(scale) = t_max;
                     }
                     h = tc_max;
                     parent = child;
@@ -740,8 +766,8 @@ __device__ V3 trace_esvo(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& 
             scale = (__float_as_uint(__uint2float_rn(dbits)) >> 23) - 127u;
             if (scale >= depth) break;  // the loop condition ends the ray
             scale_exp2 = __uint_as_float((scale - depth + 127u) << 23);
-            parent = node_stack[scale];
-            t_max = t_max_stack[scale];
+            parent = stk.n(scale);
+            t_max = stk.t(scale);
             uint32_t shx = __float_as_uint(pos.x) >> scale;
             uint32_t shy = __float_as_uint(pos.y) >> scale;
             uint32_t shz = __float_as_uint(pos.z) >> scale;
@@ -857,6 +883,9 @@ constexpr int TILE_W = 16;  // block covers 16x8 pixels: 2x2 warps of 8x4
 constexpr int TILE_H = 8;
 constexpr int BLOCK_THREADS = TILE_W * TILE_H;
 
+__device__ __forceinline__ uint32_t& EsvoSharedStack::n(uint32_t i) { return node[i * BLOCK_THREADS]; }
+__device__ __forceinline__ float& EsvoSharedStack::t(uint32_t i) { return tmax[i * BLOCK_THREADS]; }
+
 __device__ __forceinline__ bool pixel_of_thread(const Frame& f, uint32_t& ix, uint32_t& iy) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     ix = blockIdx.x * TILE_W + (warp & 1u) * 8u + (lane & 7u);
@@ -933,6 +962,24 @@ __global__ void __launch_bounds__(BLOCK_THREADS) svo_kernel(Frame f, Acc a, Outp
     write_outputs(f, o, ix, iy, color, loads, err);
 }
 
+// esvo with its stack in shared memory (23.5 KB per block of 128).
+template <bool COUNT, class Acc>
+__global__ void __launch_bounds__(BLOCK_THREADS) esvo_shared_kernel(Frame f, Acc a, Outputs o) {
+    __shared__ uint32_t s_node[STACK_DEPTH * BLOCK_THREADS];
+    __shared__ float s_tmax[STACK_DEPTH * BLOCK_THREADS];
+    uint32_t ix, iy;
+    if (!pixel_of_thread(f, ix, iy)) return;
+    EsvoSharedStack stk{s_node + threadIdx.x, s_tmax + threadIdx.x};
+    const V3 rd = primary_ray(f, ix, iy);
+    uint32_t loads = 0, err = 0;
+    // resources/esvo.comp:148-152
+    V3 ro = f.translation + vs(1.0f);
+    const float t0 = aabb_entry(vs(1.0f), vs(2.0f), ro, rd);
+    ro = ro + rd * fmaxf(t0, 0.0f);
+    const V3 total = trace_esvo<COUNT, Acc, EsvoSharedStack>(a, ro, rd, loads, err, &stk);
+    write_outputs(f, o, ix, iy, total * voxel_emission_coeff(f, rd), loads, err);
+}
+
 // Ray pool for the traversals whose work per ray varies the most (svo-df,
 // svo-naive): each warp owns a run of POOL_RAYS rays (whole 8x4 warp tiles,
 // row-major over the frame) and a lane that finishes its ray takes the warp's
@@ -952,6 +999,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) pool_kernel(Frame f, Acc a, Out
     if (begin >= total) return;
     const uint32_t end = begin + POOL_RAYS < total ? begin + POOL_RAYS : total;
     Tracer tr;
+    typename Tracer::Stack stk;
     bool active = false;
     uint32_t next = begin, ix = 0, iy = 0, loads = 0, err = 0;
     float ec = 0.0f;
@@ -969,7 +1017,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) pool_kernel(Frame f, Acc a, Out
                         ec = voxel_emission_coeff(f, rd);
                         loads = 0;
                         err = 0;
-                        active = tr.begin(a, f.translation, rd, loads);
+                        active = tr.begin(a, f.translation, rd, loads, stk);
                         if (!active) write_outputs(f, o, ix, iy, tr.result() * ec, loads, err);
                     }
                 }
@@ -980,7 +1028,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) pool_kernel(Frame f, Acc a, Out
             if (next >= end) break;
             continue;
         }
-        if (active && tr.step(a, loads, err)) {
+        if (active && tr.step(a, stk, loads, err)) {
             write_outputs(f, o, ix, iy, tr.result() * ec, loads, err);
             active = false;
         }
@@ -1038,6 +1086,16 @@ cudaError_t launch_render(const RenderLaunch& L, cudaStream_t stream) {
                   (uint64_t)L.dim[0] * L.dim[1]};
         if (count) dda_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, g, o);
         else dda_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, g, o);
+    } else if (L.traversal == XN_TRAV_ESVO && L.esvo_shared_stack) {
+        if (L.layout == XN_LAYOUT_REFERENCE) {
+            const RefNodes acc{static_cast<const uint32_t*>(L.nodes)};
+            if (count) esvo_shared_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
+            else esvo_shared_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
+        } else {
+            const CompactNodes acc{L.inner, L.inner_depth};
+            if (count) esvo_shared_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
+            else esvo_shared_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
+        }
     } else if (L.layout == XN_LAYOUT_REFERENCE) {
         launch_traversal(L.traversal, count, f, RefNodes{static_cast<const uint32_t*>(L.nodes)}, o, grid, stream);
     } else if (L.traversal == XN_TRAV_SVO_ROPE) {

@@ -46,6 +46,7 @@ struct RenderLaunch {
     const uint32_t* leaves;
     int depth_consistent;         // every internal node's depth field = its depth in the tree
     int pool;                     // svo-df / svo-naive through the ray-pool kernel (lanes refill as rays finish)
+    int esvo_shared_stack;        // esvo with its stack in shared memory
     // outputs (device pointers)
     void* d_rgba;
     float* d_emission;
