@@ -990,7 +990,7 @@ constexpr uint32_t POOL_RAYS = 256;
 
 template <int TRAV, bool COUNT, class Acc>
 __global__ void __launch_bounds__(BLOCK_THREADS) pool_kernel(Frame f, Acc a, Outputs o, uint32_t tiles_x,
-                                                             uint32_t total) {
+                                                             uint32_t total, uint32_t refill_min) {
     using Tracer = typename std::conditional<TRAV == XN_TRAV_SVO_NAIVE, NaiveTracer<COUNT, Acc>,
                                              DfTracer<COUNT, Acc>>::type;
     const uint32_t lane = threadIdx.x & 31u;
@@ -1004,8 +1004,10 @@ __global__ void __launch_bounds__(BLOCK_THREADS) pool_kernel(Frame f, Acc a, Out
     uint32_t next = begin, ix = 0, iy = 0, loads = 0, err = 0;
     float ec = 0.0f;
     for (;;) {
-        if (next < end) {
-            const unsigned idle = __ballot_sync(0xFFFFFFFFu, !active);
+        const unsigned idle = __ballot_sync(0xFFFFFFFFu, !active);
+        // refill once at least refill_min lanes are idle (or all are), so
+        // the ray set-up runs for many lanes at a time
+        if (next < end && ((uint32_t)__popc(idle) >= refill_min || idle == 0xFFFFFFFFu)) {
             if (!active) {
                 const uint32_t id = next + __popc(idle & ((1u << lane) - 1u));
                 if (id < end) {
@@ -1108,11 +1110,11 @@ cudaError_t launch_render(const RenderLaunch& L, cudaStream_t stream) {
         const dim3 blocks((total + rays_per_block - 1) / rays_per_block);
         const CompactNodes acc{L.inner, L.inner_depth};
         if (L.traversal == XN_TRAV_SVO_NAIVE) {
-            if (count) pool_kernel<XN_TRAV_SVO_NAIVE, true><<<blocks, BLOCK_THREADS, 0, stream>>>(f, acc, o, tiles_x, total);
-            else pool_kernel<XN_TRAV_SVO_NAIVE, false><<<blocks, BLOCK_THREADS, 0, stream>>>(f, acc, o, tiles_x, total);
+            if (count) pool_kernel<XN_TRAV_SVO_NAIVE, true><<<blocks, BLOCK_THREADS, 0, stream>>>(f, acc, o, tiles_x, total, L.pool);
+            else pool_kernel<XN_TRAV_SVO_NAIVE, false><<<blocks, BLOCK_THREADS, 0, stream>>>(f, acc, o, tiles_x, total, L.pool);
         } else {
-            if (count) pool_kernel<XN_TRAV_SVO_DF, true><<<blocks, BLOCK_THREADS, 0, stream>>>(f, acc, o, tiles_x, total);
-            else pool_kernel<XN_TRAV_SVO_DF, false><<<blocks, BLOCK_THREADS, 0, stream>>>(f, acc, o, tiles_x, total);
+            if (count) pool_kernel<XN_TRAV_SVO_DF, true><<<blocks, BLOCK_THREADS, 0, stream>>>(f, acc, o, tiles_x, total, L.pool);
+            else pool_kernel<XN_TRAV_SVO_DF, false><<<blocks, BLOCK_THREADS, 0, stream>>>(f, acc, o, tiles_x, total, L.pool);
         }
     } else {
         const int trav = L.traversal == XN_TRAV_SVO_DF && L.depth_consistent ? XN_TRAV_SVO_DF_MASKED : L.traversal;
