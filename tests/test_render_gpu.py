@@ -316,3 +316,21 @@ def test_esvo_stack_in_shared_memory_equals_local(ctx, blob_volumes, monkeypatch
     _, em_l, loads_l = _gpu_counts(ctx, vol, "esvo", xg.make_camera(*CAMS[cam]), p)
     assert np.array_equal(shared, local)
     assert np.array_equal(em_s, em_l) and np.array_equal(loads_s, loads_l)
+
+
+@pytest.mark.parametrize("cam", ["front", "inside", "grazing"])
+def test_dda_prefetch_depths_agree(ctx, blob_volumes, monkeypatch, cam):
+    # XN_DDA_PREFETCH=2 runs the stepping two cells ahead of the accumulation:
+    # same bits and word counts as one cell ahead, and the oracle's
+    import xenodon_gb300 as xg
+    g, _, _ = blob_volumes
+    vol = ctx.upload_grid(g)
+    p, v = _params_pair(xg, 77, 53)
+    monkeypatch.setenv("XN_DDA_PREFETCH", "2")
+    two, _ = check_parity(ctx, "dda", CAMS[cam], p, v, grid=g, vol=vol, label=f"dda-ahead2/{cam}")
+    _, em2, loads2 = _gpu_counts(ctx, vol, "dda", xg.make_camera(*CAMS[cam]), p)
+    monkeypatch.setenv("XN_DDA_PREFETCH", "1")
+    one, _, _ = ctx.render(vol, "dda", xg.make_camera(*CAMS[cam]), p)
+    _, em1, loads1 = _gpu_counts(ctx, vol, "dda", xg.make_camera(*CAMS[cam]), p)
+    assert np.array_equal(one, two)
+    assert np.array_equal(em1, em2) and np.array_equal(loads1, loads2)

@@ -18,6 +18,9 @@
 #include "../../include/xenodon.h"
 #include "xn_internal.h"
 
+#ifndef XN_DEFAULT_DDA_PREFETCH
+#define XN_DEFAULT_DDA_PREFETCH 1
+#endif
 #ifndef XN_DEFAULT_RAY_POOL
 #define XN_DEFAULT_RAY_POOL 0
 #endif
@@ -463,6 +466,9 @@ int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_p
         L.grid = v->data;
         L.tex = v->tex;
         L.tex_normalized = v->tex_normalized;
+        // texture DDA: texels fetched XN_DDA_PREFETCH (1 or 2) cells ahead
+        const char* ahead = std::getenv("XN_DDA_PREFETCH");
+        L.dda_ahead = ahead && ahead[0] == '2' ? 2 : XN_DEFAULT_DDA_PREFETCH;
     } else {
         L.nodes = v->data;
         L.layout = v->layout;

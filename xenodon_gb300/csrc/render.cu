@@ -107,7 +107,7 @@ __device__ __forceinline__ V3 tex_texel(cudaTextureObject_t t, float x, float y,
 
 // resources/dda.comp:13-53 over the texture form; coordinates are kept as
 // texel centres (integers + 0.5, exact in float).
-template <bool COUNT, bool NORM>
+template <bool COUNT, bool NORM, int AHEAD = 1>
 __device__ V3 trace_dda_tex(cudaTextureObject_t tex, uint32_t dx, uint32_t dy, uint32_t dz, V3 ro, V3 rd,
                             uint32_t& loads, uint32_t& err) {
     V3 rrd = vs(1.0f) / rd;
@@ -130,27 +130,50 @@ __device__ V3 trace_dda_tex(cudaTextureObject_t tex, uint32_t dx, uint32_t dy, u
     const float lim = t_max - t_min;
     const uint32_t cap = 2u * (dx + dy + dz) + 64u;
     uint32_t iter = 0;
-    // The texel of the next step does not depend on this one's value: fetch
-    // it before accumulating the current one so the texture latency overlaps
-    // the step arithmetic.  The fetch after the last step reads a texel the
-    // sum never uses (in range or the zero border).
-    V3 tx = tex_texel<NORM>(tex, px, py, pz);
-    while (t < lim) {
-        if (++iter > cap) { err |= 1u; break; }
+    // One step of the reference's loop body without the accumulation: the
+    // exit time of the current cell, then the move into the next one.
+    auto advance = [&]() -> float {
         const float myz = fminf(side.y, side.z);
-        bool mx = side.x <= myz;
-        bool my = side.y <= fminf(side.z, side.x);
-        bool mz = side.z <= fminf(side.x, side.y);
-        float t0 = fminf(side.x, myz);
-        if (COUNT) ++loads;
+        const bool mx = side.x <= myz;
+        const bool my = side.y <= fminf(side.z, side.x);
+        const bool mz = side.z <= fminf(side.x, side.y);
+        const float t0 = fminf(side.x, myz);
         if (mx) { side.x = side.x + t_delta.x; px += sgn.x; }
         if (my) { side.y = side.y + t_delta.y; py += sgn.y; }
         if (mz) { side.z = side.z + t_delta.z; pz += sgn.z; }
-        const V3 next = tex_texel<NORM>(tex, px, py, pz);
-        float dt = t0 - t;
-        total = total + tx * dt;
-        t = t0;
-        tx = next;
+        return t0;
+    };
+    // Texel addresses do not depend on texel values, so the stepping runs
+    // ahead of the accumulation and the texture fetches of the next AHEAD
+    // cells are in flight while a cell is accumulated.  The same operations
+    // run in the same order on the same values as in the reference's loop;
+    // fetches past the last step read texels the sum never uses (in range or
+    // the zero border).
+    V3 tx = tex_texel<NORM>(tex, px, py, pz);  // cell i
+    if (AHEAD == 1) {
+        while (t < lim) {
+            if (++iter > cap) { err |= 1u; break; }
+            if (COUNT) ++loads;
+            const float t0 = advance();
+            const V3 next = tex_texel<NORM>(tex, px, py, pz);
+            total = total + tx * (t0 - t);
+            t = t0;
+            tx = next;
+        }
+    } else {
+        float t0 = advance();                        // exit time of cell i
+        V3 tx1 = tex_texel<NORM>(tex, px, py, pz);   // cell i + 1
+        while (t < lim) {
+            if (++iter > cap) { err |= 1u; break; }
+            if (COUNT) ++loads;
+            const float t1 = advance();              // exit time of cell i + 1
+            const V3 tx2 = tex_texel<NORM>(tex, px, py, pz);
+            total = total + tx * (t0 - t);
+            t = t0;
+            tx = tx1;
+            tx1 = tx2;
+            t0 = t1;
+        }
     }
     return total;
 }
@@ -921,7 +944,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) dda_kernel(Frame f, GridVol g, 
     write_outputs(f, o, ix, iy, color, loads, err);
 }
 
-template <bool COUNT, bool NORM>
+template <bool COUNT, bool NORM, int AHEAD>
 __global__ void __launch_bounds__(BLOCK_THREADS) dda_tex_kernel(Frame f, cudaTextureObject_t tex, uint32_t dx,
                                                                uint32_t dy, uint32_t dz, Outputs o) {
     uint32_t ix, iy;
@@ -932,7 +955,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) dda_tex_kernel(Frame f, cudaTex
     V3 rd = primary_ray(f, ix, iy);
     float ec = __fdiv_rn(voxel_emission_coeff(f, rd), side);
     uint32_t loads = 0, err = 0;
-    V3 color = trace_dda_tex<COUNT, NORM>(tex, dx, dy, dz, ro, rd, loads, err) * ec;
+    V3 color = trace_dda_tex<COUNT, NORM, AHEAD>(tex, dx, dy, dz, ro, rd, loads, err) * ec;
     write_outputs(f, o, ix, iy, color, loads, err);
 }
 
@@ -1076,12 +1099,21 @@ cudaError_t launch_render(const RenderLaunch& L, cudaStream_t stream) {
     const bool count = L.d_loads != nullptr;
     if (L.traversal == XN_TRAV_DDA && L.tex) {
         const cudaTextureObject_t t = L.tex;
-        if (L.tex_normalized) {
-            if (count) dda_tex_kernel<true, true><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, L.dim[0], L.dim[1], L.dim[2], o);
-            else dda_tex_kernel<false, true><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, L.dim[0], L.dim[1], L.dim[2], o);
+        const uint32_t x = L.dim[0], y = L.dim[1], z = L.dim[2];
+        if (L.dda_ahead == 2) {
+            if (L.tex_normalized) {
+                if (count) dda_tex_kernel<true, true, 2><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+                else dda_tex_kernel<false, true, 2><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+            } else {
+                if (count) dda_tex_kernel<true, false, 2><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+                else dda_tex_kernel<false, false, 2><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+            }
+        } else if (L.tex_normalized) {
+            if (count) dda_tex_kernel<true, true, 1><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+            else dda_tex_kernel<false, true, 1><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
         } else {
-            if (count) dda_tex_kernel<true, false><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, L.dim[0], L.dim[1], L.dim[2], o);
-            else dda_tex_kernel<false, false><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, L.dim[0], L.dim[1], L.dim[2], o);
+            if (count) dda_tex_kernel<true, false, 1><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+            else dda_tex_kernel<false, false, 1><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
         }
     } else if (L.traversal == XN_TRAV_DDA) {
         GridVol g{static_cast<const uchar4*>(L.grid), L.dim[0], L.dim[1], L.dim[2], (uint64_t)L.dim[0],

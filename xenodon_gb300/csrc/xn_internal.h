@@ -48,6 +48,7 @@ struct RenderLaunch {
     int pool;                     // svo-df / svo-naive through the ray-pool kernel: 0 = off, else the least
                                   // number of idle lanes that triggers a refill (1..32)
     int esvo_shared_stack;        // esvo with its stack in shared memory
+    int dda_ahead;                // texture DDA: cells fetched ahead of the accumulation (1 or 2)
     // outputs (device pointers)
     void* d_rgba;
     float* d_emission;
