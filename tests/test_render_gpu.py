@@ -279,28 +279,6 @@ def test_parity_empty_volume_and_degenerate_regions(ctx, trav):
         check_parity(ctx, trav, CAMS["inside"], p, v, grid=g, nodes=nodes, side=st["side"], label="empty")
 
 
-@pytest.mark.parametrize("trav", ("svo-df", "svo-naive"))
-@pytest.mark.parametrize("size,refill", [((96, 64), 1), ((37, 23), 16), ((1, 1), 8), ((257, 3), 32)])
-def test_ray_pool_equals_one_ray_per_thread(ctx, blob_volumes, monkeypatch, trav, size, refill):
-    # svo-df and svo-naive in the ray-pool kernel (XN_RAY_POOL = the idle
-    # lanes that trigger a refill) must give the bits of the one-ray-per-thread
-    # kernels, and both the oracle's
-    import xenodon_gb300 as xg
-    _, nodes, side = blob_volumes
-    vol = ctx.upload_svo(nodes, side)
-    p, v = _params_pair(xg, *size)
-    for cam in ("oblique", "inside", "grazing"):
-        monkeypatch.setenv("XN_RAY_POOL", str(refill))
-        pooled, _ = check_parity(ctx, trav, CAMS[cam], p, v, nodes=nodes, vol=vol, label=f"pool/{cam}")
-        _, em_pool, loads_pool = _gpu_counts(ctx, vol, trav, xg.make_camera(*CAMS[cam]), p)
-        monkeypatch.setenv("XN_RAY_POOL", "0")
-        plain, _, _ = ctx.render(vol, trav, xg.make_camera(*CAMS[cam]), p)
-        _, em_plain, loads_plain = _gpu_counts(ctx, vol, trav, xg.make_camera(*CAMS[cam]), p)
-        monkeypatch.delenv("XN_RAY_POOL")
-        assert np.array_equal(pooled, plain), cam
-        assert np.array_equal(em_pool, em_plain) and np.array_equal(loads_pool, loads_plain), cam
-
-
 @pytest.mark.parametrize("cam", ["oblique", "inside", "grazing"])
 def test_esvo_stack_in_shared_memory_equals_local(ctx, blob_volumes, monkeypatch, cam):
     # esvo keeps its stack in shared memory by default; XN_ESVO_STACK=local

@@ -21,9 +21,6 @@
 #ifndef XN_DEFAULT_DDA_PREFETCH
 #define XN_DEFAULT_DDA_PREFETCH 1
 #endif
-#ifndef XN_DEFAULT_RAY_POOL
-#define XN_DEFAULT_RAY_POOL 0
-#endif
 #include "xn_ctx.h"
 
 namespace {
@@ -479,12 +476,6 @@ int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_p
         L.depth_consistent = v->depth_consistent;
         if (traversal == XN_TRAV_SVO_ROPE && v->layout == XN_LAYOUT_COMPACT && !v->rinner)
             return fail(XN_ERR_ARG, "svo-rope: the octree was built lean, without rope records");
-        // svo-df and svo-naive through the ray-pool kernel when XN_RAY_POOL
-        // is 1..32 (the idle lanes that trigger a refill); 0 or unset: the
-        // one-ray-per-thread kernels.  Same results either way.
-        const char* pool = std::getenv("XN_RAY_POOL");
-        const long pv = pool ? std::strtol(pool, nullptr, 10) : XN_DEFAULT_RAY_POOL;
-        L.pool = pv >= 1 && pv <= 32 ? (int)pv : 0;
         // esvo's stack in shared memory unless XN_ESVO_STACK=local
         const char* es = std::getenv("XN_ESVO_STACK");
         L.esvo_shared_stack = !(es && std::strcmp(es, "local") == 0);

@@ -12,7 +12,6 @@
 // it (where the shader would not terminate) raises a bit in the context's
 // error word instead of hanging the GPU.
 #include <cstdint>
-#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "xn_device.cuh"
@@ -356,55 +355,6 @@ __device__ V3 trace_naive(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t&
     return total;
 }
 
-// trace_naive as a resumable state machine for the ray-pool kernel (one
-// step = one find plus one colour sample); same arithmetic and order.
-template <bool COUNT, class Acc>
-struct NaiveTracer {
-    using Stack = FindPathNodes;
-    FindPath path;
-    V3 ro, rd, rrd, bias, total;
-    float t, t_max;
-    uint32_t iter;
-
-    __device__ __forceinline__ bool begin(const Acc&, V3 o, V3 d, uint32_t&, Stack&) {
-        ro = o;
-        rd = d;
-        rrd = vs(1.0f) / rd;
-        bias = rrd * ro;
-        const V3 box_min = -bias;
-        const V3 box_max = rrd - bias;
-        const float t_min = max_elem(vmin(box_min, box_max));
-        t_max = min_elem(vmax(box_min, box_max));
-        total = vs(0.0f);
-        iter = 0;
-        path.depth = -1;
-        if (t_min > t_max) return false;
-        t = fmaxf(t_min, 0.0f) + 0.00001f;
-        return t < t_max;
-    }
-
-    __device__ __forceinline__ bool step(const Acc& a, Stack& pn, uint32_t& loads, uint32_t& err) {
-        if (++iter > SVO_MAX_ITER) { err |= 1u; return true; }
-        const V3 p = rd * t + ro;
-        V3 offset;
-        float side;
-        const uint32_t node = find_cached<COUNT>(a, path, pn, p, offset, side, loads, err);
-        const V3 node_min = offset * rrd - bias;
-        const V3 node_max = (offset + vs(side)) * rrd - bias;
-        float u_min = max_elem(vmin(node_min, node_max));
-        const float u_max = min_elem(vmax(node_min, node_max));
-        u_min = fmaxf(u_min, 0.0f);
-        const float step = fmaxf(u_max - u_min, 0.00001f);
-        t += step;
-        const V3 color = unpack_rgb(a.color(node));
-        if (COUNT) ++loads;
-        total = total + color * step;
-        return !(t < t_max);
-    }
-
-    __device__ __forceinline__ V3 result() const { return total; }
-};
-
 // resources/svo_df.comp:6-67
 template <bool COUNT, class Acc>
 __device__ V3 trace_df(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& err) {
@@ -594,89 +544,6 @@ __device__ V3 trace_df_masked(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint3
     }
     return total;
 }
-
-// trace_df_masked as a resumable state machine, for the ray-pool kernel:
-// begin sets a ray up, step runs one iteration of its loop and reports whether
-// the ray is finished.  Same arithmetic and order as trace_df_masked.
-template <bool COUNT, class Acc>
-struct DfTracer {
-    // the stacks live apart from the scalar state, which stays in registers
-    struct Stack {
-        uint32_t node[STACK_DEPTH];
-        uint32_t state[STACK_DEPTH];  // remaining hit mask | depth << 8
-    };
-    V3 rrd, bias, origin, total;
-    float side;
-    uint32_t node, depth, mask, iter;
-    int sp;
-    ChildSlabs slabs;
-
-    __device__ __forceinline__ bool begin(const Acc& a, V3 ro, V3 rd, uint32_t& loads, Stack&) {
-        rrd = vs(1.0f) / rd;
-        bias = rrd * ro;
-        origin = vs(0.0f);
-        total = vs(0.0f);
-        side = 0.5f;
-        node = a.root();
-        depth = 0;
-        iter = 0;
-        sp = 0;
-        slabs = child_slabs(origin, side, rrd, bias);
-        mask = hit_mask(slabs);
-        if (COUNT) loads += 8;
-        return true;
-    }
-
-    __device__ __forceinline__ bool step(const Acc& a, Stack& stk, uint32_t& loads, uint32_t& err) {
-        if (++iter > SVO_MAX_ITER) { err |= 1u; return true; }
-        if (mask == 0) {
-            --sp;
-            if (sp < 0) return true;
-            node = stk.node[sp];
-            const uint32_t st = stk.state[sp];
-            mask = st & 0xFFu;
-            depth = st >> 8;
-            if (COUNT) ++loads;
-            side = ldexpf(1.0f, -(int)(depth > 1000u ? 1000u : depth)) * 0.5f;
-            const float s2 = side * 2.0f;
-            const float inv = __frcp_rn(s2);
-            const bool ex = pow2_with_normal_reciprocal(s2);
-            origin = origin - v3(gl_mod_pow2(origin.x, s2, inv, ex), gl_mod_pow2(origin.y, s2, inv, ex),
-                                 gl_mod_pow2(origin.z, s2, inv, ex));
-            slabs = child_slabs(origin, side, rrd, bias);
-            return false;
-        }
-        const uint32_t k = __ffs(mask) - 1;
-        mask &= mask - 1;
-        const uint32_t child = a.child(node, k);
-        if (COUNT) ++loads;
-        float t0, t1;
-        child_span(slabs, k, t0, t1);
-        if (a.is_leaf(child)) {
-            const V3 color = unpack_rgb(a.color(child));
-            if (COUNT) ++loads;
-            total = total + color * (t1 - fmaxf(t0, 0.0f));
-            return false;
-        }
-        if (k != 7) {
-            if (sp >= STACK_DEPTH) { err |= 2u; return true; }
-            stk.node[sp] = node;
-            stk.state[sp] = mask | (depth << 8);
-            ++sp;
-        }
-        origin = v3(origin.x + ((k & 4u) ? side : 0.0f), origin.y + ((k & 2u) ? side : 0.0f),
-                    origin.z + ((k & 1u) ? side : 0.0f));
-        node = child;
-        ++depth;
-        side *= 0.5f;
-        slabs = child_slabs(origin, side, rrd, bias);
-        mask = hit_mask(slabs);
-        if (COUNT) loads += 8;
-        return false;
-    }
-
-    __device__ __forceinline__ V3 result() const { return total; }
-};
 
 __device__ __forceinline__ uint32_t cxor(uint32_t x, bool ax, bool ay, bool az) {
     return x ^ (ax ? 4u : 0u) ^ (ay ? 2u : 0u) ^ (az ? 1u : 0u);
@@ -1003,63 +870,6 @@ __global__ void __launch_bounds__(BLOCK_THREADS) esvo_shared_kernel(Frame f, Acc
     write_outputs(f, o, ix, iy, total * voxel_emission_coeff(f, rd), loads, err);
 }
 
-// Ray pool for the traversals whose work per ray varies the most (svo-df,
-// svo-naive): each warp owns a run of POOL_RAYS rays (whole 8x4 warp tiles,
-// row-major over the frame) and a lane that finishes its ray takes the warp's
-// next one, so no lane idles until the longest ray of its group of 32 is
-// done.  A refill is one ballot; there is no global state, so any stream or
-// graph may launch it.
-constexpr uint32_t POOL_RAYS = 256;
-
-template <int TRAV, bool COUNT, class Acc>
-__global__ void __launch_bounds__(BLOCK_THREADS) pool_kernel(Frame f, Acc a, Outputs o, uint32_t tiles_x,
-                                                             uint32_t total, uint32_t refill_min) {
-    using Tracer = typename std::conditional<TRAV == XN_TRAV_SVO_NAIVE, NaiveTracer<COUNT, Acc>,
-                                             DfTracer<COUNT, Acc>>::type;
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t warp = blockIdx.x * (BLOCK_THREADS / 32) + (threadIdx.x >> 5);
-    const uint32_t begin = warp * POOL_RAYS;
-    if (begin >= total) return;
-    const uint32_t end = begin + POOL_RAYS < total ? begin + POOL_RAYS : total;
-    Tracer tr;
-    typename Tracer::Stack stk;
-    bool active = false;
-    uint32_t next = begin, ix = 0, iy = 0, loads = 0, err = 0;
-    float ec = 0.0f;
-    for (;;) {
-        const unsigned idle = __ballot_sync(0xFFFFFFFFu, !active);
-        // refill once at least refill_min lanes are idle (or all are), so
-        // the ray set-up runs for many lanes at a time
-        if (next < end && ((uint32_t)__popc(idle) >= refill_min || idle == 0xFFFFFFFFu)) {
-            if (!active) {
-                const uint32_t id = next + __popc(idle & ((1u << lane) - 1u));
-                if (id < end) {
-                    const uint32_t tile = id >> 5, l = id & 31u;
-                    ix = (tile % tiles_x) * 8u + (l & 7u);
-                    iy = (tile / tiles_x) * 4u + (l >> 3);
-                    if (ix < f.out_w && iy < f.out_h) {
-                        const V3 rd = primary_ray(f, ix, iy);
-                        ec = voxel_emission_coeff(f, rd);
-                        loads = 0;
-                        err = 0;
-                        active = tr.begin(a, f.translation, rd, loads, stk);
-                        if (!active) write_outputs(f, o, ix, iy, tr.result() * ec, loads, err);
-                    }
-                }
-            }
-            next += __popc(idle);
-        }
-        if (!__any_sync(0xFFFFFFFFu, active)) {
-            if (next >= end) break;
-            continue;
-        }
-        if (active && tr.step(a, stk, loads, err)) {
-            write_outputs(f, o, ix, iy, tr.result() * ec, loads, err);
-            active = false;
-        }
-    }
-}
-
 template <int TRAV, class Acc>
 static void launch_svo_any(bool count, const Frame& f, const Acc& a, const Outputs& o, dim3 grid, cudaStream_t s) {
     if (count) svo_kernel<TRAV, true, Acc><<<grid, BLOCK_THREADS, 0, s>>>(f, a, o);
@@ -1134,20 +944,6 @@ cudaError_t launch_render(const RenderLaunch& L, cudaStream_t stream) {
         launch_traversal(L.traversal, count, f, RefNodes{static_cast<const uint32_t*>(L.nodes)}, o, grid, stream);
     } else if (L.traversal == XN_TRAV_SVO_ROPE) {
         launch_traversal(L.traversal, count, f, RopeNodes{L.rinner, L.inner_depth, L.leaves}, o, grid, stream);
-    } else if (L.pool && ((L.traversal == XN_TRAV_SVO_DF && L.depth_consistent) ||
-                          L.traversal == XN_TRAV_SVO_NAIVE)) {
-        const uint32_t tiles_x = (L.out_w + 7) / 8, tiles_y = (L.out_h + 3) / 4;
-        const uint32_t total = tiles_x * tiles_y * 32u;
-        const uint32_t rays_per_block = POOL_RAYS * (BLOCK_THREADS / 32);
-        const dim3 blocks((total + rays_per_block - 1) / rays_per_block);
-        const CompactNodes acc{L.inner, L.inner_depth};
-        if (L.traversal == XN_TRAV_SVO_NAIVE) {
-            if (count) pool_kernel<XN_TRAV_SVO_NAIVE, true><<<blocks, BLOCK_THREADS, 0, stream>>>(f, acc, o, tiles_x, total, L.pool);
-            else pool_kernel<XN_TRAV_SVO_NAIVE, false><<<blocks, BLOCK_THREADS, 0, stream>>>(f, acc, o, tiles_x, total, L.pool);
-        } else {
-            if (count) pool_kernel<XN_TRAV_SVO_DF, true><<<blocks, BLOCK_THREADS, 0, stream>>>(f, acc, o, tiles_x, total, L.pool);
-            else pool_kernel<XN_TRAV_SVO_DF, false><<<blocks, BLOCK_THREADS, 0, stream>>>(f, acc, o, tiles_x, total, L.pool);
-        }
     } else {
         const int trav = L.traversal == XN_TRAV_SVO_DF && L.depth_consistent ? XN_TRAV_SVO_DF_MASKED : L.traversal;
         launch_traversal(trav, count, f, CompactNodes{L.inner, L.inner_depth}, o, grid, stream);

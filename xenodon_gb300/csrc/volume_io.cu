@@ -69,10 +69,12 @@ struct File {
     }
 };
 
-// Two pinned chunk buffers with an event each.
+// Two pinned chunk buffers with an event each; pending[k]: a copy from or to
+// buffer k may still be running (shared by every array streamed through them).
 struct Staging {
     void* buf[2] = {nullptr, nullptr};
     cudaEvent_t ev[2] = {nullptr, nullptr};
+    bool pending[2] = {false, false};
     ~Staging() {
         for (int k = 0; k < 2; ++k) {
             if (ev[k]) {
@@ -116,17 +118,16 @@ int stream_out(cudaStream_t s, Staging& st, std::FILE* f, const void* d, uint64_
 int stream_in(cudaStream_t s, Staging& st, std::FILE* f, void* d, uint64_t bytes, const char* path) {
     char* dst = static_cast<char*>(d);
     const uint64_t n = (bytes + CHUNK - 1) / CHUNK;
-    bool pending[2] = {false, false};
     for (uint64_t i = 0; i < n; ++i) {
         const int k = (int)(i & 1);
-        if (pending[k] && cudaEventSynchronize(st.ev[k]) != cudaSuccess)
+        if (st.pending[k] && cudaEventSynchronize(st.ev[k]) != cudaSuccess)
             return fail(XN_ERR_CUDA, "'%s': device write failed", path);
         const uint64_t off = i * CHUNK, take = bytes - off < CHUNK ? bytes - off : CHUNK;
         if (std::fread(st.buf[k], 1, take, f) != take) return fail(XN_ERR_IO, "'%s': short read", path);
         if (cudaMemcpyAsync(dst + off, st.buf[k], take, cudaMemcpyHostToDevice, s) != cudaSuccess ||
             cudaEventRecord(st.ev[k], s) != cudaSuccess)
             return fail(XN_ERR_CUDA, "'%s': device write failed", path);
-        pending[k] = true;
+        st.pending[k] = true;
     }
     return XN_OK;
 }

@@ -45,8 +45,6 @@ struct RenderLaunch {
     const uint32_t* inner_depth;
     const uint32_t* leaves;
     int depth_consistent;         // every internal node's depth field = its depth in the tree
-    int pool;                     // svo-df / svo-naive through the ray-pool kernel: 0 = off, else the least
-                                  // number of idle lanes that triggers a refill (1..32)
     int esvo_shared_stack;        // esvo with its stack in shared memory
     int dda_ahead;                // texture DDA: cells fetched ahead of the accumulation (1 or 2)
     // outputs (device pointers)
