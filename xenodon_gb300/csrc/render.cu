@@ -456,13 +456,23 @@ __device__ __forceinline__ void child_span(const ChildSlabs& c, uint32_t k, floa
     t1 = fminf(bx ? c.xh1 : c.xh0, fminf(by ? c.yh1 : c.yh0, bz ? c.zh1 : c.zh0));
 }
 
+// fmaxf/fminf are exact and the slab values are finite (every ray direction
+// component is at least 2^-23 in magnitude), so the per-child max/min may be
+// grouped as max(max(x, y), z): the x-y part is shared by the two children
+// that differ only in z.
 __device__ __forceinline__ uint32_t hit_mask(const ChildSlabs& c) {
     uint32_t m = 0;
 #pragma unroll
-    for (uint32_t k = 0; k < 8; ++k) {
-        float t0, t1;
-        child_span(c, k, t0, t1);
-        if (t0 < t1 && t1 > 0.0f) m |= 1u << k;
+    for (uint32_t xy = 0; xy < 4; ++xy) {
+        const bool bx = xy & 2u, by = xy & 1u;
+        const float lo = fmaxf(bx ? c.xl1 : c.xl0, by ? c.yl1 : c.yl0);
+        const float hi = fminf(bx ? c.xh1 : c.xh0, by ? c.yh1 : c.yh0);
+#pragma unroll
+        for (uint32_t bz = 0; bz < 2; ++bz) {
+            const float t0 = fmaxf(lo, bz ? c.zl1 : c.zl0);
+            const float t1 = fminf(hi, bz ? c.zh1 : c.zh0);
+            if (t0 < t1 && t1 > 0.0f) m |= 1u << (xy * 2u + bz);
+        }
     }
     return m;
 }
@@ -505,10 +515,21 @@ __device__ V3 trace_df_masked(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint3
             mask = st & 0xFFu;
             depth = st >> 8;
             if (COUNT) ++loads;
-            side = ldexpf(1.0f, -(int)(depth > 1000u ? 1000u : depth)) * 0.5f;
-            const float s2 = side * 2.0f;
-            const float inv = __frcp_rn(s2);
-            const bool ex = pow2_with_normal_reciprocal(s2);
+            float s2, inv;
+            bool ex;
+            if (depth <= 124u) {
+                // 2^-depth and 2^depth built from their exponents: the values
+                // ldexpf and the correctly rounded reciprocal give
+                s2 = __uint_as_float((127u - depth) << 23);
+                inv = __uint_as_float((127u + depth) << 23);
+                side = s2 * 0.5f;
+                ex = true;
+            } else {
+                side = ldexpf(1.0f, -(int)(depth > 1000u ? 1000u : depth)) * 0.5f;
+                s2 = side * 2.0f;
+                inv = __frcp_rn(s2);
+                ex = pow2_with_normal_reciprocal(s2);
+            }
             origin = origin - v3(gl_mod_pow2(origin.x, s2, inv, ex), gl_mod_pow2(origin.y, s2, inv, ex),
                                  gl_mod_pow2(origin.z, s2, inv, ex));
             slabs = child_slabs(origin, side, rrd, bias);
