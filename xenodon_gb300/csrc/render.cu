@@ -264,58 +264,87 @@ struct FindPathNodes {
     uint32_t node[PATH_CACHE];
 };
 struct FindPath {
-    int depth = -1;  // depth of the last leaf found, -1: none (or too deep to cache)
-    V3 base;         // the last leaf's origin
+    int depth = -1;          // depth of the last leaf found, -1: none (or too deep to cache)
+    uint32_t cx, cy, cz;     // the last leaf's origin in units of 2^-FIX_BITS
 };
 
-__device__ __forceinline__ bool in_capture(float p, float o, float size) {
-    return (o == 0.0f || p >= o) && (o + size == 1.0f || p < o + size);
+// Positions in fixed point: a coordinate p becomes clamp(floor(p * 2^30), 0,
+// 2^30 - 1).  For a node at depth j <= 24 with origin O (a multiple of 2^-j),
+// "p >= O + 2^-(j+1)" (the reference's descent test) is bit 29-j of that
+// integer, and the capture region of the node (its box, with a bound at
+// -inf/+inf where it is the root's) holds p exactly when the top j bits of
+// the integer equal O's: the clamp supplies the open bounds.  Origins and
+// extents of depth <= 24 are exact floats either way.
+constexpr int FIX_BITS = 30;
+constexpr int FIX_DEPTH = 24;
+
+__device__ __forceinline__ uint32_t fix_coord(float p) {
+    const float q = floorf(fminf(fmaxf(p, -1.0f), 1.5f) * 1073741824.0f);  // * 2^30, exact
+    const int v = (int)q;
+    return (uint32_t)min(max(v, 0), (1 << FIX_BITS) - 1);
 }
+
+__device__ __forceinline__ float fix_to_float(uint32_t v) { return (float)v * (1.0f / 1073741824.0f); }
 
 template <bool COUNT, class Acc>
 __device__ __forceinline__ uint32_t find_cached(const Acc& a, FindPath& path, FindPathNodes& pn, V3 pos, V3& base,
                                                 float& side, uint32_t& loads, uint32_t& err) {
+    const uint32_t px = fix_coord(pos.x), py = fix_coord(pos.y), pz = fix_coord(pos.z);
     int level = 0;
-    float extent = 1.0f;
     uint32_t index = a.root();
-    V3 offset = vs(0.0f);
-    for (int j = path.depth; j > 0; --j) {
-        const float size = ldexpf(1.0f, -j);
-        const float inv = ldexpf(1.0f, j);
-        const V3 o = v3(floorf(path.base.x * inv) * size, floorf(path.base.y * inv) * size,
-                        floorf(path.base.z * inv) * size);
-        if (in_capture(pos.x, o.x, size) && in_capture(pos.y, o.y, size) && in_capture(pos.z, o.z, size)) {
+    if (path.depth > 0) {
+        // the deepest level of the last path whose capture region holds p:
+        // the number of leading bits p shares with the last leaf's origin
+        const uint32_t diff = (px ^ path.cx) | (py ^ path.cy) | (pz ^ path.cz);
+        int j = diff ? __clz(diff) - (32 - FIX_BITS) : FIX_BITS;
+        if (j > path.depth) j = path.depth;
+        if (j >= 1) {
             level = j;
-            extent = size;
             index = pn.node[j];
-            offset = o;
-            break;
         }
     }
     for (;; ++level) {
         if (level < PATH_CACHE) pn.node[level] = index;
-        if (a.is_leaf(index)) {
-            base = offset;
-            side = extent;
-            if (COUNT) loads += 2u * (uint32_t)level + 1u;
-            path.depth = level < PATH_CACHE ? level : -1;
-            path.base = offset;
-            return index;
-        }
-        if (level >= FIND_MAX_DEPTH) {
-            err |= 1u;
-            base = offset;
-            side = extent;
-            path.depth = -1;
-            return index;
-        }
-        extent *= 0.5f;
-        V3 oe = offset + vs(extent);
-        bool mx = pos.x >= oe.x, my = pos.y >= oe.y, mz = pos.z >= oe.z;
-        uint32_t child = (mx ? 4u : 0u) | (my ? 2u : 0u) | (mz ? 1u : 0u);
-        offset = offset + v3(mx ? 1.0f : 0.0f, my ? 1.0f : 0.0f, mz ? 1.0f : 0.0f) * vs(extent);
-        index = a.child(index, child);
+        if (a.is_leaf(index) || level == FIX_DEPTH) break;
+        const int b = FIX_BITS - 1 - level;
+        const uint32_t k = (((px >> b) & 1u) << 2) | (((py >> b) & 1u) << 1) | ((pz >> b) & 1u);
+        index = a.child(index, k);
     }
+    const uint32_t keep = ~((1u << (FIX_BITS - level)) - 1u);
+    V3 offset = v3(fix_to_float(px & keep), fix_to_float(py & keep), fix_to_float(pz & keep));
+    float extent = __uint_as_float((uint32_t)(127 - level) << 23);  // 2^-level
+    if (!a.is_leaf(index)) {
+        // below depth 24 (deeper than any grid of 2^24 voxels per axis): the
+        // reference's float descent
+        for (;; ++level) {
+            if (level < PATH_CACHE) pn.node[level] = index;
+            if (a.is_leaf(index)) break;
+            if (level >= FIND_MAX_DEPTH) {
+                err |= 1u;
+                base = offset;
+                side = extent;
+                path.depth = -1;
+                return index;
+            }
+            extent *= 0.5f;
+            const V3 oe = offset + vs(extent);
+            const bool mx = pos.x >= oe.x, my = pos.y >= oe.y, mz = pos.z >= oe.z;
+            offset = offset + v3(mx ? 1.0f : 0.0f, my ? 1.0f : 0.0f, mz ? 1.0f : 0.0f) * vs(extent);
+            index = a.child(index, (mx ? 4u : 0u) | (my ? 2u : 0u) | (mz ? 1u : 0u));
+        }
+    }
+    base = offset;
+    side = extent;
+    if (COUNT) loads += 2u * (uint32_t)level + 1u;
+    if (level <= FIX_DEPTH && level < PATH_CACHE) {
+        path.depth = level;
+        path.cx = px & keep;
+        path.cy = py & keep;
+        path.cz = pz & keep;
+    } else {
+        path.depth = -1;
+    }
+    return index;
 }
 
 // resources/svo_naive.comp:29-71
