@@ -725,9 +725,19 @@ __device__ __forceinline__ uint32_t find_relative(const Acc& a, uint32_t parent,
                                                   float& side, uint32_t& loads, uint32_t& err) {
     uint32_t d = a.depth(parent);
     if (COUNT) ++loads;
-    float extent = ldexpf(1.0f, -(int)(d > 1000u ? 1000u : d));
-    offset = v3(offset.x - gl_mod(offset.x, extent), offset.y - gl_mod(offset.y, extent),
-                offset.z - gl_mod(offset.z, extent));
+    // mod by extent = 2^-d: for d <= 124 the division is the exact multiply
+    // by 2^d (both built from their exponents), as in gl_mod_pow2
+    float extent, inv = 0.0f;
+    bool ex = false;
+    if (d <= 124u) {
+        extent = __uint_as_float((127u - d) << 23);
+        inv = __uint_as_float((127u + d) << 23);
+        ex = true;
+    } else {
+        extent = ldexpf(1.0f, -(int)(d > 1000u ? 1000u : d));
+    }
+    offset = v3(offset.x - gl_mod_pow2(offset.x, extent, inv, ex), offset.y - gl_mod_pow2(offset.y, extent, inv, ex),
+                offset.z - gl_mod_pow2(offset.z, extent, inv, ex));
     for (int level = 0;; ++level) {
         if (COUNT) ++loads;
         if (a.is_leaf(parent)) {
