@@ -131,3 +131,26 @@ def test_batch_rejects_bad_shapes_and_jobs(ctx, scene):
     bad = ctx.make_jobs([(vols["grid"], "esvo", specs[0][2], specs[0][3], bufs[0].data_ptr())])
     with pytest.raises(xg.XenodonError):
         ctx.render_batch(bad, 1)
+
+
+@pytest.mark.parametrize("vname,trav", [("grid", "dda"), ("svo", "svo-naive"), ("svo", "esvo"), ("svo", "svo-df"),
+                                        ("svo", "svo-rope")])
+def test_single_traversal_batches_use_the_inlined_form(ctx, scene, monkeypatch, vname, trav):
+    # a batch whose jobs share one traversal runs a kernel with that
+    # traversal inlined; it must equal the single-frame renders and the
+    # generic form (XN_BATCH_GENERIC=1)
+    import torch
+    xg, vols = scene
+    specs = [(vols[vname], trav, xg.make_camera(*CAMS[i % len(CAMS)]), xg.make_params(*SIZES[i % len(SIZES)], 10.0))
+             for i in range(6)]
+    ref = _reference_frames(ctx, specs)
+    stream = torch.cuda.current_stream().cuda_stream
+    for generic in ("0", "1"):
+        monkeypatch.setenv("XN_BATCH_GENERIC", generic)
+        for cfg in (xg.BatchConfig(8, 128, 0, 1), xg.BatchConfig(4, 64, 0, 3)):
+            bufs = _batch_buffers(specs)
+            jobs = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs, bufs))
+            ctx.render_batch(jobs, len(specs), cfg, stream)
+            torch.cuda.synchronize()
+            for b, r in zip(bufs, ref):
+                assert np.array_equal(b.cpu().numpy(), r), (trav, generic)

@@ -34,7 +34,7 @@ int check_config(const xn_batch_config& c) {
 
 // Builds header + jobs into `table`; returns the byte size.
 int fill_table(Ctx* c, const xn_job* jobs, int n, uint32_t tile_w, void* table, uint64_t capacity_bytes,
-               uint64_t* bytes_out) {
+               uint64_t* bytes_out, int* spec_out = nullptr) {
     const uint64_t need = sizeof(BatchHeader) + (uint64_t)n * sizeof(BatchJob);
     if (need > capacity_bytes) return fail(XN_ERR_ARG, "batch: %d jobs exceed the job table capacity", n);
     BatchHeader* h = static_cast<BatchHeader*>(table);
@@ -55,6 +55,8 @@ int fill_table(Ctx* c, const xn_job* jobs, int n, uint32_t tile_w, void* table, 
         out[i].tiles_y = (L.out_h + tile_h - 1) / tile_h;
         out[i].tile_begin = tiles;
         tiles += (unsigned long long)out[i].tiles_x * out[i].tiles_y;
+        const int sp = batch_spec(out[i]);
+        if (spec_out) *spec_out = i == 0 ? sp : (*spec_out == sp ? sp : XN_BATCH_ANY);
     }
     h->n_jobs = (uint32_t)n;
     h->pad = 0;
@@ -101,7 +103,11 @@ int render_batch_locked(Ctx* c, const xn_job* jobs, int n, const xn_batch_config
     cudaError_t e = cudaEventSynchronize(c->batch_copied);  // the previous table left the staging buffer
     if (e != cudaSuccess) return cuda_fail(e, "xn_render_batch: staging");
     uint64_t bytes = 0;
-    if ((r = fill_table(c, jobs, n, cfg.tile_width, c->batch_host, c->batch_host_bytes, &bytes))) return r;
+    int spec = XN_BATCH_ANY;
+    if ((r = fill_table(c, jobs, n, cfg.tile_width, c->batch_host, c->batch_host_bytes, &bytes, &spec))) return r;
+    // XN_BATCH_GENERIC=1 keeps the generic form (same results)
+    const char* generic = std::getenv("XN_BATCH_GENERIC");
+    if (generic && generic[0] == '1') spec = XN_BATCH_ANY;
     const uint64_t queue_off = (bytes + 255) & ~255ull;
     void* d = nullptr;
     e = cudaMallocAsync(&d, queue_off + 256, s);
@@ -111,7 +117,8 @@ int render_batch_locked(Ctx* c, const xn_job* jobs, int n, const xn_batch_config
     if (e == cudaSuccess) e = cudaEventRecord(c->batch_copied, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(queue, 0, 8, s);
     if (e == cudaSuccess)
-        e = launch_batch(d, queue, c->d_err, cfg.tile_width, cfg.block_threads, resident_blocks(c, cfg), cfg.chunk, s);
+        e = launch_batch(d, queue, c->d_err, cfg.tile_width, cfg.block_threads, resident_blocks(c, cfg), cfg.chunk, spec,
+                         s);
     const cudaError_t ef = cudaFreeAsync(d, s);
     if (e == cudaSuccess) e = ef;
     return e == cudaSuccess ? XN_OK : cuda_fail(e, "xn_render_batch");
@@ -201,6 +208,7 @@ struct xn_batch_graph {
     Ctx* ctx;
     cudaStream_t stream;
     xn_batch_config cfg;
+    int spec = XN_BATCH_ANY;  // captured once for any jobs: the generic form
     int capacity;
     uint64_t table_bytes;
     struct Slot {
@@ -266,7 +274,8 @@ XN_API int xn_batch_graph_create(xn_ctx* h, int capacity, const xn_batch_config*
         if ((e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
         cudaMemcpyAsync(sl.dev, sl.host, g->table_bytes, cudaMemcpyHostToDevice, cap);
         cudaMemsetAsync(sl.queue, 0, 8, cap);
-        launch_batch(sl.dev, sl.queue, c->d_err, g->cfg.tile_width, g->cfg.block_threads, blocks, g->cfg.chunk, cap);
+        launch_batch(sl.dev, sl.queue, c->d_err, g->cfg.tile_width, g->cfg.block_threads, blocks, g->cfg.chunk,
+                     g->spec, cap);
         cudaGraph_t graph = nullptr;
         e = cudaStreamEndCapture(cap, &graph);
         if (e == cudaSuccess) e = cudaGraphInstantiate(&sl.exec, graph, 0);

@@ -1057,6 +1057,19 @@ BatchJob make_batch_job(const RenderLaunch& L) {
     return j;
 }
 
+int batch_spec(const BatchJob& j) {
+    if (j.traversal == XN_TRAV_DDA)
+        return j.layout == 1 ? (j.tex_normalized ? XN_BATCH_DDA_TEX_NORM : XN_BATCH_DDA_TEX_RAW) : XN_BATCH_ANY;
+    if (j.layout != XN_LAYOUT_COMPACT) return XN_BATCH_ANY;
+    switch (j.traversal) {
+    case XN_TRAV_ESVO: return XN_BATCH_ESVO;
+    case XN_TRAV_SVO_NAIVE: return XN_BATCH_NAIVE;
+    case XN_TRAV_SVO_DF: return j.depth_consistent ? XN_BATCH_DF : XN_BATCH_ANY;
+    case XN_TRAV_SVO_ROPE: return XN_BATCH_ROPE;
+    default: return XN_BATCH_ANY;
+    }
+}
+
 __device__ __forceinline__ Frame frame_of(const BatchJob& J) {
     Frame f;
     f.forward = v3(J.forward[0], J.forward[1], J.forward[2]);
@@ -1143,7 +1156,39 @@ __device__ __noinline__ uint32_t render_job_pixel(const BatchJob& J, uint32_t ix
     return pack_rgba(color);
 }
 
-template <int TW>
+// One pixel of a job whose traversal and layout the whole batch shares
+// (BatchSpec): that traversal inlined, the arithmetic of render_job_pixel.
+template <int SPEC>
+__device__ __forceinline__ uint32_t render_job_pixel_spec(const BatchJob& J, uint32_t ix, uint32_t iy, uint32_t& err) {
+    if constexpr (SPEC == XN_BATCH_ANY) {
+        return render_job_pixel(J, ix, iy, err);
+    } else {
+        const Frame f = frame_of(J);
+        const V3 rd = primary_ray(f, ix, iy);
+        uint32_t loads = 0;
+        V3 color;
+        if constexpr (SPEC == XN_BATCH_DDA_TEX_NORM || SPEC == XN_BATCH_DDA_TEX_RAW) {
+            const uint32_t m = max(J.dim[0], max(J.dim[1], J.dim[2]));
+            const float side = (float)m;
+            const V3 ro = f.translation * side;
+            const float ec = __fdiv_rn(voxel_emission_coeff(f, rd), side);
+            color = trace_dda_tex<false, SPEC == XN_BATCH_DDA_TEX_NORM>(J.tex, J.dim[0], J.dim[1], J.dim[2], ro, rd,
+                                                                        loads, err) * ec;
+        } else if constexpr (SPEC == XN_BATCH_ROPE) {
+            color = trace_svo_job<XN_TRAV_SVO_ROPE>(RopeNodes{J.rinner, J.inner_depth, J.leaves}, f, rd, loads, err) *
+                    voxel_emission_coeff(f, rd);
+        } else {
+            constexpr int TRAV = SPEC == XN_BATCH_ESVO ? XN_TRAV_ESVO
+                                 : SPEC == XN_BATCH_NAIVE ? XN_TRAV_SVO_NAIVE
+                                                          : XN_TRAV_SVO_DF_MASKED;
+            color = trace_svo_job<TRAV>(CompactNodes{J.inner, J.inner_depth}, f, rd, loads, err) *
+                    voxel_emission_coeff(f, rd);
+        }
+        return pack_rgba(color);
+    }
+}
+
+template <int TW, int SPEC>
 __global__ void __launch_bounds__(1024) batch_kernel(const BatchHeader* hdr, const BatchJob* jobs,
                                                      unsigned long long* queue, uint32_t chunk, uint32_t* err_word) {
     constexpr int TH = 32 / TW;
@@ -1170,7 +1215,7 @@ __global__ void __launch_bounds__(1024) batch_kernel(const BatchHeader* hdr, con
             const uint32_t tx = (uint32_t)(local - (unsigned long long)ty * J.tiles_x);
             const uint32_t ix = tx * TW + lane % TW, iy = ty * TH + lane / TW;
             if (ix < J.out_w && iy < J.out_h) {
-                const uint32_t px = render_job_pixel(J, ix, iy, err);
+                const uint32_t px = render_job_pixel_spec<SPEC>(J, ix, iy, err);
                 static_cast<uint32_t*>(J.rgba)[(uint64_t)iy * J.out_w + ix] = px;
             }
         }
@@ -1178,33 +1223,49 @@ __global__ void __launch_bounds__(1024) batch_kernel(const BatchHeader* hdr, con
     if (err) atomicOr(err_word, err);
 }
 
-template <int TW>
-static cudaError_t launch_batch_tw(const void* table, unsigned long long* q, uint32_t* err, uint32_t threads,
-                                   uint32_t blocks, uint32_t chunk, cudaStream_t s) {
+template <int TW, int SPEC>
+static cudaError_t launch_batch_tws(const void* table, unsigned long long* q, uint32_t* err, uint32_t threads,
+                                    uint32_t blocks, uint32_t chunk, cudaStream_t s) {
     const BatchHeader* hdr = static_cast<const BatchHeader*>(table);
     const BatchJob* jobs = reinterpret_cast<const BatchJob*>(hdr + 1);
-    batch_kernel<TW><<<blocks, threads, 0, s>>>(hdr, jobs, q, chunk, err);
+    batch_kernel<TW, SPEC><<<blocks, threads, 0, s>>>(hdr, jobs, q, chunk, err);
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch(const void* table, unsigned long long* q, uint32_t* err, uint32_t tile_w,
-                         uint32_t threads, uint32_t blocks, uint32_t chunk, cudaStream_t s) {
-    switch (tile_w) {
-    case 4: return launch_batch_tw<4>(table, q, err, threads, blocks, chunk, s);
-    case 16: return launch_batch_tw<16>(table, q, err, threads, blocks, chunk, s);
-    case 32: return launch_batch_tw<32>(table, q, err, threads, blocks, chunk, s);
-    default: return launch_batch_tw<8>(table, q, err, threads, blocks, chunk, s);
+template <int TW>
+static cudaError_t launch_batch_tw(const void* table, unsigned long long* q, uint32_t* err, uint32_t threads,
+                                   uint32_t blocks, uint32_t chunk, int spec, cudaStream_t s) {
+    switch (spec) {
+    case XN_BATCH_DDA_TEX_NORM: return launch_batch_tws<TW, XN_BATCH_DDA_TEX_NORM>(table, q, err, threads, blocks, chunk, s);
+    case XN_BATCH_DDA_TEX_RAW: return launch_batch_tws<TW, XN_BATCH_DDA_TEX_RAW>(table, q, err, threads, blocks, chunk, s);
+    case XN_BATCH_ESVO: return launch_batch_tws<TW, XN_BATCH_ESVO>(table, q, err, threads, blocks, chunk, s);
+    case XN_BATCH_NAIVE: return launch_batch_tws<TW, XN_BATCH_NAIVE>(table, q, err, threads, blocks, chunk, s);
+    case XN_BATCH_DF: return launch_batch_tws<TW, XN_BATCH_DF>(table, q, err, threads, blocks, chunk, s);
+    case XN_BATCH_ROPE: return launch_batch_tws<TW, XN_BATCH_ROPE>(table, q, err, threads, blocks, chunk, s);
+    default: return launch_batch_tws<TW, XN_BATCH_ANY>(table, q, err, threads, blocks, chunk, s);
     }
 }
 
+cudaError_t launch_batch(const void* table, unsigned long long* q, uint32_t* err, uint32_t tile_w,
+                         uint32_t threads, uint32_t blocks, uint32_t chunk, int spec, cudaStream_t s) {
+    switch (tile_w) {
+    case 4: return launch_batch_tw<4>(table, q, err, threads, blocks, chunk, spec, s);
+    case 16: return launch_batch_tw<16>(table, q, err, threads, blocks, chunk, spec, s);
+    case 32: return launch_batch_tw<32>(table, q, err, threads, blocks, chunk, spec, s);
+    default: return launch_batch_tw<8>(table, q, err, threads, blocks, chunk, spec, s);
+    }
+}
+
+// Resident blocks per SM of the generic kernel (the most demanding of the
+// forms, so the specialised ones fit the same grid).
 int batch_kernel_blocks_per_sm(uint32_t tile_w, uint32_t threads) {
     int n = 0;
     cudaError_t e;
     switch (tile_w) {
-    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<4>, (int)threads, 0); break;
-    case 16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<16>, (int)threads, 0); break;
-    case 32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<32>, (int)threads, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<8>, (int)threads, 0); break;
+    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<4, XN_BATCH_ANY>, (int)threads, 0); break;
+    case 16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<16, XN_BATCH_ANY>, (int)threads, 0); break;
+    case 32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<32, XN_BATCH_ANY>, (int)threads, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<8, XN_BATCH_ANY>, (int)threads, 0); break;
     }
     return e == cudaSuccess ? n : 0;
 }

@@ -88,11 +88,18 @@ struct alignas(16) BatchHeader {
 };
 
 BatchJob make_batch_job(const RenderLaunch& L);
+// Batch kernel forms: one traversal (and layout) inlined when every job of
+// the batch shares it, else the generic per-pixel dispatch.
+enum { XN_BATCH_ANY = 0, XN_BATCH_DDA_TEX_NORM, XN_BATCH_DDA_TEX_RAW, XN_BATCH_ESVO, XN_BATCH_NAIVE, XN_BATCH_DF,
+       XN_BATCH_ROPE };
+// The form a job needs (XN_BATCH_*).
+int batch_spec(const BatchJob& j);
 // Launches the persistent kernel over a job table already in device memory
 // (header followed by the jobs).  tile_w is the warp tile's width in pixels
-// (4, 8, 16 or 32; height 32/tile_w).
+// (4, 8, 16 or 32; height 32/tile_w); spec is the form every job shares, or
+// XN_BATCH_ANY.
 cudaError_t launch_batch(const void* d_table, unsigned long long* d_queue, uint32_t* d_err, uint32_t tile_w,
-                         uint32_t block_threads, uint32_t blocks, uint32_t chunk, cudaStream_t stream);
+                         uint32_t threads, uint32_t blocks, uint32_t chunk, int spec, cudaStream_t s);
 int batch_kernel_blocks_per_sm(uint32_t tile_w, uint32_t block_threads);
 
 }  // namespace xn
