@@ -279,36 +279,37 @@ def test_parity_empty_volume_and_degenerate_regions(ctx, trav):
         check_parity(ctx, trav, CAMS["inside"], p, v, grid=g, nodes=nodes, side=st["side"], label="empty")
 
 
+@pytest.mark.parametrize("trav", ["esvo", "svo-df"])
 @pytest.mark.parametrize("cam", ["oblique", "inside", "grazing"])
-def test_esvo_stack_in_shared_memory_equals_local(ctx, blob_volumes, monkeypatch, cam):
-    # esvo keeps its stack in shared memory by default; XN_ESVO_STACK=local
-    # selects the local-memory form: same bits, same word counts
+def test_stacks_in_shared_memory_equal_local(ctx, blob_volumes, monkeypatch, trav, cam):
+    # esvo and the masked svo-df keep their stacks in shared memory by
+    # default; XN_STACKS=local selects the local-memory form: same bits,
+    # same word counts
     import xenodon_gb300 as xg
     _, nodes, side = blob_volumes
     vol = ctx.upload_svo(nodes, side)
     p, v = _params_pair(xg, 83, 61)
-    shared, _ = check_parity(ctx, "esvo", CAMS[cam], p, v, nodes=nodes, vol=vol, label=f"esvo-shared/{cam}")
-    _, em_s, loads_s = _gpu_counts(ctx, vol, "esvo", xg.make_camera(*CAMS[cam]), p)
-    monkeypatch.setenv("XN_ESVO_STACK", "local")
-    local, _, _ = ctx.render(vol, "esvo", xg.make_camera(*CAMS[cam]), p)
-    _, em_l, loads_l = _gpu_counts(ctx, vol, "esvo", xg.make_camera(*CAMS[cam]), p)
+    shared, _ = check_parity(ctx, trav, CAMS[cam], p, v, nodes=nodes, vol=vol, label=f"{trav}-shared/{cam}")
+    _, em_s, loads_s = _gpu_counts(ctx, vol, trav, xg.make_camera(*CAMS[cam]), p)
+    monkeypatch.setenv("XN_STACKS", "local")
+    local, _, _ = ctx.render(vol, trav, xg.make_camera(*CAMS[cam]), p)
+    _, em_l, loads_l = _gpu_counts(ctx, vol, trav, xg.make_camera(*CAMS[cam]), p)
     assert np.array_equal(shared, local)
     assert np.array_equal(em_s, em_l) and np.array_equal(loads_s, loads_l)
 
 
-@pytest.mark.parametrize("cam", ["front", "inside", "grazing"])
-def test_dda_prefetch_depths_agree(ctx, blob_volumes, monkeypatch, cam):
-    # XN_DDA_PREFETCH=2 runs the stepping two cells ahead of the accumulation:
-    # same bits and word counts as one cell ahead, and the oracle's
+@pytest.mark.parametrize("cam", ["oblique", "inside", "grazing", "front"])
+def test_naive_resumed_find_equals_root_descent(ctx, blob_volumes, monkeypatch, cam):
+    # svo-naive resumes each find from the previous path (fixed point);
+    # XN_NAIVE_FIND=root descends from the root like the reference: same bits
     import xenodon_gb300 as xg
-    g, _, _ = blob_volumes
-    vol = ctx.upload_grid(g)
-    p, v = _params_pair(xg, 77, 53)
-    monkeypatch.setenv("XN_DDA_PREFETCH", "2")
-    two, _ = check_parity(ctx, "dda", CAMS[cam], p, v, grid=g, vol=vol, label=f"dda-ahead2/{cam}")
-    _, em2, loads2 = _gpu_counts(ctx, vol, "dda", xg.make_camera(*CAMS[cam]), p)
-    monkeypatch.setenv("XN_DDA_PREFETCH", "1")
-    one, _, _ = ctx.render(vol, "dda", xg.make_camera(*CAMS[cam]), p)
-    _, em1, loads1 = _gpu_counts(ctx, vol, "dda", xg.make_camera(*CAMS[cam]), p)
-    assert np.array_equal(one, two)
-    assert np.array_equal(em1, em2) and np.array_equal(loads1, loads2)
+    _, nodes, side = blob_volumes
+    vol = ctx.upload_svo(nodes, side)
+    p, v = _params_pair(xg, 91, 47)
+    resumed, _ = check_parity(ctx, "svo-naive", CAMS[cam], p, v, nodes=nodes, vol=vol, label=f"naive/{cam}")
+    _, em_r, loads_r = _gpu_counts(ctx, vol, "svo-naive", xg.make_camera(*CAMS[cam]), p)
+    monkeypatch.setenv("XN_NAIVE_FIND", "root")
+    root, _, _ = ctx.render(vol, "svo-naive", xg.make_camera(*CAMS[cam]), p)
+    _, em_0, loads_0 = _gpu_counts(ctx, vol, "svo-naive", xg.make_camera(*CAMS[cam]), p)
+    assert np.array_equal(resumed, root)
+    assert np.array_equal(em_r, em_0) and np.array_equal(loads_r, loads_0)

@@ -18,9 +18,6 @@
 #include "../../include/xenodon.h"
 #include "xn_internal.h"
 
-#ifndef XN_DEFAULT_DDA_PREFETCH
-#define XN_DEFAULT_DDA_PREFETCH 1
-#endif
 #include "xn_ctx.h"
 
 namespace {
@@ -463,9 +460,6 @@ int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_p
         L.grid = v->data;
         L.tex = v->tex;
         L.tex_normalized = v->tex_normalized;
-        // texture DDA: texels fetched XN_DDA_PREFETCH (1 or 2) cells ahead
-        const char* ahead = std::getenv("XN_DDA_PREFETCH");
-        L.dda_ahead = ahead && ahead[0] == '2' ? 2 : XN_DEFAULT_DDA_PREFETCH;
     } else {
         L.nodes = v->data;
         L.layout = v->layout;
@@ -476,9 +470,12 @@ int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_p
         L.depth_consistent = v->depth_consistent;
         if (traversal == XN_TRAV_SVO_ROPE && v->layout == XN_LAYOUT_COMPACT && !v->rinner)
             return fail(XN_ERR_ARG, "svo-rope: the octree was built lean, without rope records");
-        // esvo's stack in shared memory unless XN_ESVO_STACK=local
-        const char* es = std::getenv("XN_ESVO_STACK");
-        L.esvo_shared_stack = !(es && std::strcmp(es, "local") == 0);
+        // esvo's and svo-df's stacks in shared memory unless XN_STACKS=local
+        const char* es = std::getenv("XN_STACKS");
+        L.shared_stacks = !(es && std::strcmp(es, "local") == 0);
+        // svo-naive's find resumes from the last path unless XN_NAIVE_FIND=root
+        const char* nf = std::getenv("XN_NAIVE_FIND");
+        L.naive_resume = !(nf && std::strcmp(nf, "root") == 0);
     }
     for (int i = 0; i < 3; ++i) L.dim[i] = v->dim[i];
     return XN_OK;

@@ -72,10 +72,12 @@ __device__ V3 trace_dda(const GridVol& g, V3 ro, V3 rd, uint32_t& loads, uint32_
     uint32_t iter = 0;
     while (t < lim) {
         if (++iter > cap) { err |= 1u; break; }
-        bool mx = side.x <= fminf(side.y, side.z);
-        bool my = side.y <= fminf(side.z, side.x);
-        bool mz = side.z <= fminf(side.x, side.y);
+        // lessThanEqual(side, min(side.yzx, side.zxy)) is side.k == min of
+        // all three (the sides are finite and positive)
         float t0 = min_elem(side);
+        bool mx = side.x == t0;
+        bool my = side.y == t0;
+        bool mz = side.z == t0;
         V3 tx = fetch_texel(g, px, py, pz);
         if (COUNT) ++loads;
         float dt = t0 - t;
@@ -106,7 +108,7 @@ __device__ __forceinline__ V3 tex_texel(cudaTextureObject_t t, float x, float y,
 
 // resources/dda.comp:13-53 over the texture form; coordinates are kept as
 // texel centres (integers + 0.5, exact in float).
-template <bool COUNT, bool NORM, int AHEAD = 1>
+template <bool COUNT, bool NORM>
 __device__ V3 trace_dda_tex(cudaTextureObject_t tex, uint32_t dx, uint32_t dy, uint32_t dz, V3 ro, V3 rd,
                             uint32_t& loads, uint32_t& err) {
     V3 rrd = vs(1.0f) / rd;
@@ -129,50 +131,24 @@ __device__ V3 trace_dda_tex(cudaTextureObject_t tex, uint32_t dx, uint32_t dy, u
     const float lim = t_max - t_min;
     const uint32_t cap = 2u * (dx + dy + dz) + 64u;
     uint32_t iter = 0;
-    // One step of the reference's loop body without the accumulation: the
-    // exit time of the current cell, then the move into the next one.
-    auto advance = [&]() -> float {
-        const float myz = fminf(side.y, side.z);
-        const bool mx = side.x <= myz;
-        const bool my = side.y <= fminf(side.z, side.x);
-        const bool mz = side.z <= fminf(side.x, side.y);
-        const float t0 = fminf(side.x, myz);
-        if (mx) { side.x = side.x + t_delta.x; px += sgn.x; }
-        if (my) { side.y = side.y + t_delta.y; py += sgn.y; }
-        if (mz) { side.z = side.z + t_delta.z; pz += sgn.z; }
-        return t0;
-    };
-    // Texel addresses do not depend on texel values, so the stepping runs
-    // ahead of the accumulation and the texture fetches of the next AHEAD
-    // cells are in flight while a cell is accumulated.  The same operations
-    // run in the same order on the same values as in the reference's loop;
-    // fetches past the last step read texels the sum never uses (in range or
-    // the zero border).
-    V3 tx = tex_texel<NORM>(tex, px, py, pz);  // cell i
-    if (AHEAD == 1) {
-        while (t < lim) {
-            if (++iter > cap) { err |= 1u; break; }
-            if (COUNT) ++loads;
-            const float t0 = advance();
-            const V3 next = tex_texel<NORM>(tex, px, py, pz);
-            total = total + tx * (t0 - t);
-            t = t0;
-            tx = next;
-        }
-    } else {
-        float t0 = advance();                        // exit time of cell i
-        V3 tx1 = tex_texel<NORM>(tex, px, py, pz);   // cell i + 1
-        while (t < lim) {
-            if (++iter > cap) { err |= 1u; break; }
-            if (COUNT) ++loads;
-            const float t1 = advance();              // exit time of cell i + 1
-            const V3 tx2 = tex_texel<NORM>(tex, px, py, pz);
-            total = total + tx * (t0 - t);
-            t = t0;
-            tx = tx1;
-            tx1 = tx2;
-            t0 = t1;
-        }
+    // The texel of the next step does not depend on this one's value: fetch
+    // it before accumulating the current one so the texture latency overlaps
+    // the step arithmetic.  The fetch after the last step reads a texel the
+    // sum never uses (in range or the zero border).
+    V3 tx = tex_texel<NORM>(tex, px, py, pz);
+    while (t < lim) {
+        if (++iter > cap) { err |= 1u; break; }
+        if (COUNT) ++loads;
+        // lessThanEqual(side, min(side.yzx, side.zxy)) is side.k == min of
+        // all three (the sides are finite and positive)
+        const float t0 = fminf(side.x, fminf(side.y, side.z));
+        if (side.x == t0) { side.x = side.x + t_delta.x; px += sgn.x; }
+        if (side.y == t0) { side.y = side.y + t_delta.y; py += sgn.y; }
+        if (side.z == t0) { side.z = side.z + t_delta.z; pz += sgn.z; }
+        const V3 next = tex_texel<NORM>(tex, px, py, pz);
+        total = total + tx * (t0 - t);
+        t = t0;
+        tx = next;
     }
     return total;
 }
@@ -347,8 +323,10 @@ __device__ __forceinline__ uint32_t find_cached(const Acc& a, FindPath& path, Fi
     return index;
 }
 
-// resources/svo_naive.comp:29-71
-template <bool COUNT, class Acc>
+// resources/svo_naive.comp:29-71.  RESUME: each step's find resumes from the
+// previous path (find_cached); else it descends from the root (find), as the
+// reference does.  Both find the same node with the same base and side.
+template <bool COUNT, class Acc, bool RESUME = true>
 __device__ V3 trace_naive(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& err) {
     const float MIN_STEP = 0.00001f;
     V3 rrd = vs(1.0f) / rd;
@@ -369,7 +347,8 @@ __device__ V3 trace_naive(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t&
         V3 p = rd * t + ro;
         V3 offset;
         float side;
-        uint32_t node = find_cached<COUNT>(a, path, pn, p, offset, side, loads, err);
+        uint32_t node = RESUME ? find_cached<COUNT>(a, path, pn, p, offset, side, loads, err)
+                               : find<COUNT>(a, p, offset, side, loads, err);
         V3 node_min = offset * rrd - bias;
         V3 node_max = (offset + vs(side)) * rrd - bias;
         float u_min = max_elem(vmin(node_min, node_max));
@@ -452,6 +431,25 @@ __device__ V3 trace_df(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& er
     return total;
 }
 
+// Two 32-bit stacks of STACK_DEPTH entries per thread (svo-df: node and
+// remaining mask | depth; esvo: parent and t_max bits), in local memory or in
+// shared memory with one column per thread (entry i of a thread at i * stride
+// from its column start, so a warp touching one entry hits 32 banks).
+struct LocalStacks {
+    uint32_t a[STACK_DEPTH];
+    uint32_t b[STACK_DEPTH];
+    __device__ __forceinline__ uint32_t& first(uint32_t i) { return a[i]; }
+    __device__ __forceinline__ uint32_t& second(uint32_t i) { return b[i]; }
+};
+
+struct SharedStacks {
+    uint32_t* a;  // this thread's column in each array
+    uint32_t* b;
+    uint32_t stride;
+    __device__ __forceinline__ uint32_t& first(uint32_t i) { return a[i * stride]; }
+    __device__ __forceinline__ uint32_t& second(uint32_t i) { return b[i * stride]; }
+};
+
 // resources/svo_df.comp:6-67 for octrees whose depth fields match the tree
 // (checked on upload; every octree the reference's builder writes does).
 // The reference tests the 8 child boxes of a node one loop iteration at a
@@ -517,12 +515,13 @@ __device__ __forceinline__ uint32_t hit_mask(const ChildSlabs& c) {
 // happen exactly where the reference's do, the accumulation order and every
 // accumulated value are the reference's, so the result is bit-identical, and
 // so is the count of words the reference reads.
-template <bool COUNT, class Acc>
-__device__ V3 trace_df_masked(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& err) {
+template <bool COUNT, class Acc, class Stacks = LocalStacks>
+__device__ V3 trace_df_masked(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& err,
+                              Stacks* shared_stacks = nullptr) {
     const V3 rrd = vs(1.0f) / rd;
     const V3 bias = rrd * ro;
-    uint32_t node_stack[STACK_DEPTH];
-    uint32_t state_stack[STACK_DEPTH];  // remaining hit mask | depth << 8
+    Stacks local;
+    Stacks& stk = shared_stacks ? *shared_stacks : local;  // first: node, second: remaining mask | depth << 8
     int sp = 0;
     uint32_t node = a.root();
     uint32_t depth = 0;
@@ -539,8 +538,8 @@ __device__ V3 trace_df_masked(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint3
             // node finished: the reference pops, reading the parent's depth
             --sp;
             if (sp < 0) break;
-            node = node_stack[sp];
-            const uint32_t st = state_stack[sp];
+            node = stk.first(sp);
+            const uint32_t st = stk.second(sp);
             mask = st & 0xFFu;
             depth = st >> 8;
             if (COUNT) ++loads;
@@ -579,8 +578,8 @@ __device__ V3 trace_df_masked(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint3
         // descend into child k; the reference pushes unless k == 7
         if (k != 7) {
             if (sp >= STACK_DEPTH) { err |= 2u; break; }
-            node_stack[sp] = node;
-            state_stack[sp] = mask | (depth << 8);
+            stk.first(sp) = node;
+            stk.second(sp) = mask | (depth << 8);
             ++sp;
         }
         origin = v3(origin.x + ((k & 4u) ? side : 0.0f), origin.y + ((k & 2u) ? side : 0.0f),
@@ -600,30 +599,15 @@ __device__ __forceinline__ uint32_t cxor(uint32_t x, bool ax, bool ay, bool az) 
 }
 
 // resources/esvo.comp:30-136
-// ESVO's (parent, t_max) stack, indexed by scale: in local memory, or in
-// shared memory with one column per thread (entry i of thread t at
-// i * BLOCK_THREADS + t, so a warp touching one scale hits 32 banks).
-struct EsvoLocalStack {
-    uint32_t node[STACK_DEPTH];
-    float tmax[STACK_DEPTH];
-    __device__ __forceinline__ uint32_t& n(uint32_t i) { return node[i]; }
-    __device__ __forceinline__ float& t(uint32_t i) { return tmax[i]; }
-};
-
-struct EsvoSharedStack {
-    uint32_t* node;  // this thread's column
-    float* tmax;
-    __device__ __forceinline__ uint32_t& n(uint32_t i);
-    __device__ __forceinline__ float& t(uint32_t i);
-};
-
-template <bool COUNT, class Acc, class Stack = EsvoLocalStack>
-__device__ V3 trace_esvo(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& err, Stack* shared_stack = nullptr) {
+// ESVO's (parent, t_max) stack, indexed by scale: LocalStacks / SharedStacks
+// (t_max kept as its bits).
+template <bool COUNT, class Acc, class Stacks = LocalStacks>
+__device__ V3 trace_esvo(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& err, Stacks* shared_stacks = nullptr) {
     const uint32_t depth = STACK_DEPTH;
-    Stack local;
-    Stack& stk = shared_stack ? *shared_stack : local;
+    Stacks local;
+    Stacks& stk = shared_stacks ? *shared_stacks : local;  // first: parent, second: t_max bits
 #pragma unroll
-    for (int i = 0; i < STACK_DEPTH; ++i) { stk.n(i) = 0; stk.t(i) = 0.0f; }
+    for (int i = 0; i < STACK_DEPTH; ++i) { stk.first(i) = 0; stk.second(i) = 0u; }
 
     V3 t_coeff = v3(1.0f / -fabsf(rd.x), 1.0f / -fabsf(rd.y), 1.0f / -fabsf(rd.z));
     V3 t_bias = t_coeff * ro;
@@ -671,8 +655,8 @@ __device__ V3 trace_esvo(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& 
                     total = total + color * (tv_max - t_min);
                 } else {
                     if (tc_max < h) {
-                        stk.n(scale) = parent;
-                        stk.t(scale) = t_max;
+                        stk.first(scale) = parent;
+                        stk.second(scale) = __float_as_uint(t_max);
                     }
                     h = tc_max;
                     parent = child;
@@ -706,8 +690,8 @@ __device__ V3 trace_esvo(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& 
             scale = (__float_as_uint(__uint2float_rn(dbits)) >> 23) - 127u;
             if (scale >= depth) break;  // the loop condition ends the ray
             scale_exp2 = __uint_as_float((scale - depth + 127u) << 23);
-            parent = stk.n(scale);
-            t_max = stk.t(scale);
+            parent = stk.first(scale);
+            t_max = __uint_as_float(stk.second(scale));
             uint32_t shx = __float_as_uint(pos.x) >> scale;
             uint32_t shy = __float_as_uint(pos.y) >> scale;
             uint32_t shz = __float_as_uint(pos.z) >> scale;
@@ -833,8 +817,6 @@ constexpr int TILE_W = 16;  // block covers 16x8 pixels: 2x2 warps of 8x4
 constexpr int TILE_H = 8;
 constexpr int BLOCK_THREADS = TILE_W * TILE_H;
 
-__device__ __forceinline__ uint32_t& EsvoSharedStack::n(uint32_t i) { return node[i * BLOCK_THREADS]; }
-__device__ __forceinline__ float& EsvoSharedStack::t(uint32_t i) { return tmax[i * BLOCK_THREADS]; }
 
 __device__ __forceinline__ bool pixel_of_thread(const Frame& f, uint32_t& ix, uint32_t& iy) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -871,7 +853,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) dda_kernel(Frame f, GridVol g, 
     write_outputs(f, o, ix, iy, color, loads, err);
 }
 
-template <bool COUNT, bool NORM, int AHEAD>
+template <bool COUNT, bool NORM>
 __global__ void __launch_bounds__(BLOCK_THREADS) dda_tex_kernel(Frame f, cudaTextureObject_t tex, uint32_t dx,
                                                                uint32_t dy, uint32_t dz, Outputs o) {
     uint32_t ix, iy;
@@ -882,7 +864,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) dda_tex_kernel(Frame f, cudaTex
     V3 rd = primary_ray(f, ix, iy);
     float ec = __fdiv_rn(voxel_emission_coeff(f, rd), side);
     uint32_t loads = 0, err = 0;
-    V3 color = trace_dda_tex<COUNT, NORM, AHEAD>(tex, dx, dy, dz, ro, rd, loads, err) * ec;
+    V3 color = trace_dda_tex<COUNT, NORM>(tex, dx, dy, dz, ro, rd, loads, err) * ec;
     write_outputs(f, o, ix, iy, color, loads, err);
 }
 
@@ -901,6 +883,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS) svo_kernel(Frame f, Acc a, Outp
         total = trace_esvo<COUNT>(a, ro, rd, loads, err);
     } else if (TRAV == XN_TRAV_SVO_NAIVE) {
         total = trace_naive<COUNT>(a, f.translation, rd, loads, err);
+    } else if (TRAV == XN_TRAV_SVO_NAIVE_ROOT) {
+        total = trace_naive<COUNT, Acc, false>(a, f.translation, rd, loads, err);
     } else if (TRAV == XN_TRAV_SVO_DF) {
         total = trace_df<COUNT>(a, f.translation, rd, loads, err);
     } else if (TRAV == XN_TRAV_SVO_DF_MASKED) {
@@ -912,21 +896,27 @@ __global__ void __launch_bounds__(BLOCK_THREADS) svo_kernel(Frame f, Acc a, Outp
     write_outputs(f, o, ix, iy, color, loads, err);
 }
 
-// esvo with its stack in shared memory (23.5 KB per block of 128).
-template <bool COUNT, class Acc>
-__global__ void __launch_bounds__(BLOCK_THREADS) esvo_shared_kernel(Frame f, Acc a, Outputs o) {
-    __shared__ uint32_t s_node[STACK_DEPTH * BLOCK_THREADS];
-    __shared__ float s_tmax[STACK_DEPTH * BLOCK_THREADS];
+// esvo and the masked svo-df with their stacks in shared memory (23.5 KB per
+// block of 128).
+template <int TRAV, bool COUNT, class Acc>
+__global__ void __launch_bounds__(BLOCK_THREADS) shared_stack_kernel(Frame f, Acc a, Outputs o) {
+    __shared__ uint32_t s_a[STACK_DEPTH * BLOCK_THREADS];
+    __shared__ uint32_t s_b[STACK_DEPTH * BLOCK_THREADS];
     uint32_t ix, iy;
     if (!pixel_of_thread(f, ix, iy)) return;
-    EsvoSharedStack stk{s_node + threadIdx.x, s_tmax + threadIdx.x};
+    SharedStacks stk{s_a + threadIdx.x, s_b + threadIdx.x, BLOCK_THREADS};
     const V3 rd = primary_ray(f, ix, iy);
     uint32_t loads = 0, err = 0;
-    // resources/esvo.comp:148-152
-    V3 ro = f.translation + vs(1.0f);
-    const float t0 = aabb_entry(vs(1.0f), vs(2.0f), ro, rd);
-    ro = ro + rd * fmaxf(t0, 0.0f);
-    const V3 total = trace_esvo<COUNT, Acc, EsvoSharedStack>(a, ro, rd, loads, err, &stk);
+    V3 total;
+    if constexpr (TRAV == XN_TRAV_ESVO) {
+        // resources/esvo.comp:148-152
+        V3 ro = f.translation + vs(1.0f);
+        const float t0 = aabb_entry(vs(1.0f), vs(2.0f), ro, rd);
+        ro = ro + rd * fmaxf(t0, 0.0f);
+        total = trace_esvo<COUNT, Acc, SharedStacks>(a, ro, rd, loads, err, &stk);
+    } else {
+        total = trace_df_masked<COUNT, Acc, SharedStacks>(a, f.translation, rd, loads, err, &stk);
+    }
     write_outputs(f, o, ix, iy, total * voxel_emission_coeff(f, rd), loads, err);
 }
 
@@ -941,6 +931,7 @@ static void launch_traversal(int traversal, bool count, const Frame& f, const Ac
                              cudaStream_t s) {
     switch (traversal) {
     case XN_TRAV_SVO_NAIVE: launch_svo_any<XN_TRAV_SVO_NAIVE>(count, f, a, o, grid, s); break;
+    case XN_TRAV_SVO_NAIVE_ROOT: launch_svo_any<XN_TRAV_SVO_NAIVE_ROOT>(count, f, a, o, grid, s); break;
     case XN_TRAV_ESVO: launch_svo_any<XN_TRAV_ESVO>(count, f, a, o, grid, s); break;
     case XN_TRAV_SVO_DF: launch_svo_any<XN_TRAV_SVO_DF>(count, f, a, o, grid, s); break;
     case XN_TRAV_SVO_DF_MASKED: launch_svo_any<XN_TRAV_SVO_DF_MASKED>(count, f, a, o, grid, s); break;
@@ -970,42 +961,40 @@ cudaError_t launch_render(const RenderLaunch& L, cudaStream_t stream) {
     if (L.traversal == XN_TRAV_DDA && L.tex) {
         const cudaTextureObject_t t = L.tex;
         const uint32_t x = L.dim[0], y = L.dim[1], z = L.dim[2];
-        if (L.dda_ahead == 2) {
-            if (L.tex_normalized) {
-                if (count) dda_tex_kernel<true, true, 2><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
-                else dda_tex_kernel<false, true, 2><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
-            } else {
-                if (count) dda_tex_kernel<true, false, 2><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
-                else dda_tex_kernel<false, false, 2><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
-            }
-        } else if (L.tex_normalized) {
-            if (count) dda_tex_kernel<true, true, 1><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
-            else dda_tex_kernel<false, true, 1><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+        if (L.tex_normalized) {
+            if (count) dda_tex_kernel<true, true><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+            else dda_tex_kernel<false, true><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
         } else {
-            if (count) dda_tex_kernel<true, false, 1><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
-            else dda_tex_kernel<false, false, 1><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+            if (count) dda_tex_kernel<true, false><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+            else dda_tex_kernel<false, false><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
         }
     } else if (L.traversal == XN_TRAV_DDA) {
         GridVol g{static_cast<const uchar4*>(L.grid), L.dim[0], L.dim[1], L.dim[2], (uint64_t)L.dim[0],
                   (uint64_t)L.dim[0] * L.dim[1]};
         if (count) dda_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, g, o);
         else dda_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, g, o);
-    } else if (L.traversal == XN_TRAV_ESVO && L.esvo_shared_stack) {
+    } else if (L.traversal == XN_TRAV_ESVO && L.shared_stacks) {
         if (L.layout == XN_LAYOUT_REFERENCE) {
             const RefNodes acc{static_cast<const uint32_t*>(L.nodes)};
-            if (count) esvo_shared_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
-            else esvo_shared_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
+            if (count) shared_stack_kernel<XN_TRAV_ESVO, true><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
+            else shared_stack_kernel<XN_TRAV_ESVO, false><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
         } else {
             const CompactNodes acc{L.inner, L.inner_depth};
-            if (count) esvo_shared_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
-            else esvo_shared_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
+            if (count) shared_stack_kernel<XN_TRAV_ESVO, true><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
+            else shared_stack_kernel<XN_TRAV_ESVO, false><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
         }
+    } else if (L.traversal == XN_TRAV_SVO_DF && L.shared_stacks && L.layout == XN_LAYOUT_COMPACT &&
+               L.depth_consistent) {
+        const CompactNodes acc{L.inner, L.inner_depth};
+        if (count) shared_stack_kernel<XN_TRAV_SVO_DF_MASKED, true><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
+        else shared_stack_kernel<XN_TRAV_SVO_DF_MASKED, false><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
     } else if (L.layout == XN_LAYOUT_REFERENCE) {
         launch_traversal(L.traversal, count, f, RefNodes{static_cast<const uint32_t*>(L.nodes)}, o, grid, stream);
     } else if (L.traversal == XN_TRAV_SVO_ROPE) {
         launch_traversal(L.traversal, count, f, RopeNodes{L.rinner, L.inner_depth, L.leaves}, o, grid, stream);
     } else {
-        const int trav = L.traversal == XN_TRAV_SVO_DF && L.depth_consistent ? XN_TRAV_SVO_DF_MASKED : L.traversal;
+        int trav = L.traversal == XN_TRAV_SVO_DF && L.depth_consistent ? XN_TRAV_SVO_DF_MASKED : L.traversal;
+        if (trav == XN_TRAV_SVO_NAIVE && !L.naive_resume) trav = XN_TRAV_SVO_NAIVE_ROOT;
         launch_traversal(trav, count, f, CompactNodes{L.inner, L.inner_depth}, o, grid, stream);
     }
     return cudaGetLastError();
@@ -1090,24 +1079,26 @@ __device__ __forceinline__ Frame frame_of(const BatchJob& J) {
 }
 
 template <int TRAV, class Acc>
-__device__ __forceinline__ V3 trace_svo_job(const Acc& a, const Frame& f, V3 rd, uint32_t& loads, uint32_t& err) {
+__device__ __forceinline__ V3 trace_svo_job(const Acc& a, const Frame& f, V3 rd, uint32_t& loads, uint32_t& err,
+                                            SharedStacks* stk) {
     if (TRAV == XN_TRAV_ESVO) {
         V3 ro = f.translation + vs(1.0f);
         float t0 = aabb_entry(vs(1.0f), vs(2.0f), ro, rd);
         ro = ro + rd * fmaxf(t0, 0.0f);
-        return trace_esvo<false>(a, ro, rd, loads, err);
+        return trace_esvo<false, Acc, SharedStacks>(a, ro, rd, loads, err, stk);
     } else if (TRAV == XN_TRAV_SVO_NAIVE) {
         return trace_naive<false>(a, f.translation, rd, loads, err);
     } else if (TRAV == XN_TRAV_SVO_DF) {
         return trace_df<false>(a, f.translation, rd, loads, err);
     } else if (TRAV == XN_TRAV_SVO_DF_MASKED) {
-        return trace_df_masked<false>(a, f.translation, rd, loads, err);
+        return trace_df_masked<false, Acc, SharedStacks>(a, f.translation, rd, loads, err, stk);
     }
     return trace_rope<false>(a, f.translation, rd, loads, err);
 }
 
 // One pixel of one job: the same arithmetic as the single-frame kernels.
-__device__ __noinline__ uint32_t render_job_pixel(const BatchJob& J, uint32_t ix, uint32_t iy, uint32_t& err) {
+__device__ __noinline__ uint32_t render_job_pixel(const BatchJob& J, uint32_t ix, uint32_t iy, uint32_t& err,
+                                                  SharedStacks* stk) {
     const Frame f = frame_of(J);
     const V3 rd = primary_ray(f, ix, iy);
     uint32_t loads = 0;
@@ -1133,21 +1124,22 @@ __device__ __noinline__ uint32_t render_job_pixel(const BatchJob& J, uint32_t ix
         if (J.layout == XN_LAYOUT_REFERENCE) {
             RefNodes a{static_cast<const uint32_t*>(J.nodes)};
             switch (J.traversal) {
-            case XN_TRAV_SVO_NAIVE: total = trace_svo_job<XN_TRAV_SVO_NAIVE>(a, f, rd, loads, err); break;
-            case XN_TRAV_ESVO: total = trace_svo_job<XN_TRAV_ESVO>(a, f, rd, loads, err); break;
-            case XN_TRAV_SVO_DF: total = trace_svo_job<XN_TRAV_SVO_DF>(a, f, rd, loads, err); break;
-            default: total = trace_svo_job<XN_TRAV_SVO_ROPE>(a, f, rd, loads, err); break;
+            case XN_TRAV_SVO_NAIVE: total = trace_svo_job<XN_TRAV_SVO_NAIVE>(a, f, rd, loads, err, stk); break;
+            case XN_TRAV_ESVO: total = trace_svo_job<XN_TRAV_ESVO>(a, f, rd, loads, err, stk); break;
+            case XN_TRAV_SVO_DF: total = trace_svo_job<XN_TRAV_SVO_DF>(a, f, rd, loads, err, stk); break;
+            default: total = trace_svo_job<XN_TRAV_SVO_ROPE>(a, f, rd, loads, err, stk); break;
             }
         } else if (J.traversal == XN_TRAV_SVO_ROPE) {
-            total = trace_svo_job<XN_TRAV_SVO_ROPE>(RopeNodes{J.rinner, J.inner_depth, J.leaves}, f, rd, loads, err);
+            total = trace_svo_job<XN_TRAV_SVO_ROPE>(RopeNodes{J.rinner, J.inner_depth, J.leaves}, f, rd, loads, err,
+                                                    stk);
         } else {
             CompactNodes a{J.inner, J.inner_depth};
             switch (J.traversal) {
-            case XN_TRAV_SVO_NAIVE: total = trace_svo_job<XN_TRAV_SVO_NAIVE>(a, f, rd, loads, err); break;
-            case XN_TRAV_ESVO: total = trace_svo_job<XN_TRAV_ESVO>(a, f, rd, loads, err); break;
+            case XN_TRAV_SVO_NAIVE: total = trace_svo_job<XN_TRAV_SVO_NAIVE>(a, f, rd, loads, err, stk); break;
+            case XN_TRAV_ESVO: total = trace_svo_job<XN_TRAV_ESVO>(a, f, rd, loads, err, stk); break;
             default:
-                total = J.depth_consistent ? trace_svo_job<XN_TRAV_SVO_DF_MASKED>(a, f, rd, loads, err)
-                                           : trace_svo_job<XN_TRAV_SVO_DF>(a, f, rd, loads, err);
+                total = J.depth_consistent ? trace_svo_job<XN_TRAV_SVO_DF_MASKED>(a, f, rd, loads, err, stk)
+                                           : trace_svo_job<XN_TRAV_SVO_DF>(a, f, rd, loads, err, stk);
                 break;
             }
         }
@@ -1159,9 +1151,10 @@ __device__ __noinline__ uint32_t render_job_pixel(const BatchJob& J, uint32_t ix
 // One pixel of a job whose traversal and layout the whole batch shares
 // (BatchSpec): that traversal inlined, the arithmetic of render_job_pixel.
 template <int SPEC>
-__device__ __forceinline__ uint32_t render_job_pixel_spec(const BatchJob& J, uint32_t ix, uint32_t iy, uint32_t& err) {
+__device__ __forceinline__ uint32_t render_job_pixel_spec(const BatchJob& J, uint32_t ix, uint32_t iy, uint32_t& err,
+                                                          SharedStacks* stk) {
     if constexpr (SPEC == XN_BATCH_ANY) {
-        return render_job_pixel(J, ix, iy, err);
+        return render_job_pixel(J, ix, iy, err, stk);
     } else {
         const Frame f = frame_of(J);
         const V3 rd = primary_ray(f, ix, iy);
@@ -1175,13 +1168,14 @@ __device__ __forceinline__ uint32_t render_job_pixel_spec(const BatchJob& J, uin
             color = trace_dda_tex<false, SPEC == XN_BATCH_DDA_TEX_NORM>(J.tex, J.dim[0], J.dim[1], J.dim[2], ro, rd,
                                                                         loads, err) * ec;
         } else if constexpr (SPEC == XN_BATCH_ROPE) {
-            color = trace_svo_job<XN_TRAV_SVO_ROPE>(RopeNodes{J.rinner, J.inner_depth, J.leaves}, f, rd, loads, err) *
+            color = trace_svo_job<XN_TRAV_SVO_ROPE>(RopeNodes{J.rinner, J.inner_depth, J.leaves}, f, rd, loads, err,
+                                                    stk) *
                     voxel_emission_coeff(f, rd);
         } else {
             constexpr int TRAV = SPEC == XN_BATCH_ESVO ? XN_TRAV_ESVO
                                  : SPEC == XN_BATCH_NAIVE ? XN_TRAV_SVO_NAIVE
                                                           : XN_TRAV_SVO_DF_MASKED;
-            color = trace_svo_job<TRAV>(CompactNodes{J.inner, J.inner_depth}, f, rd, loads, err) *
+            color = trace_svo_job<TRAV>(CompactNodes{J.inner, J.inner_depth}, f, rd, loads, err, stk) *
                     voxel_emission_coeff(f, rd);
         }
         return pack_rgba(color);
@@ -1192,6 +1186,10 @@ template <int TW, int SPEC>
 __global__ void __launch_bounds__(1024) batch_kernel(const BatchHeader* hdr, const BatchJob* jobs,
                                                      unsigned long long* queue, uint32_t chunk, uint32_t* err_word) {
     constexpr int TH = 32 / TW;
+    // esvo and svo-df stacks: two columns per thread in dynamic shared memory
+    // (2 * STACK_DEPTH words a thread, given at launch for the forms that use them)
+    extern __shared__ uint32_t batch_stacks[];
+    SharedStacks stk{batch_stacks + threadIdx.x, batch_stacks + STACK_DEPTH * blockDim.x + threadIdx.x, blockDim.x};
     const uint32_t lane = threadIdx.x & 31u;
     const unsigned long long total = hdr->total_tiles;
     const uint32_t n = hdr->n_jobs;
@@ -1215,7 +1213,7 @@ __global__ void __launch_bounds__(1024) batch_kernel(const BatchHeader* hdr, con
             const uint32_t tx = (uint32_t)(local - (unsigned long long)ty * J.tiles_x);
             const uint32_t ix = tx * TW + lane % TW, iy = ty * TH + lane / TW;
             if (ix < J.out_w && iy < J.out_h) {
-                const uint32_t px = render_job_pixel_spec<SPEC>(J, ix, iy, err);
+                const uint32_t px = render_job_pixel_spec<SPEC>(J, ix, iy, err, &stk);
                 static_cast<uint32_t*>(J.rgba)[(uint64_t)iy * J.out_w + ix] = px;
             }
         }
@@ -1223,12 +1221,22 @@ __global__ void __launch_bounds__(1024) batch_kernel(const BatchHeader* hdr, con
     if (err) atomicOr(err_word, err);
 }
 
+constexpr bool batch_needs_stacks(int spec) {
+    return spec == XN_BATCH_ANY || spec == XN_BATCH_ESVO || spec == XN_BATCH_DF;
+}
+
 template <int TW, int SPEC>
 static cudaError_t launch_batch_tws(const void* table, unsigned long long* q, uint32_t* err, uint32_t threads,
                                     uint32_t blocks, uint32_t chunk, cudaStream_t s) {
     const BatchHeader* hdr = static_cast<const BatchHeader*>(table);
     const BatchJob* jobs = reinterpret_cast<const BatchJob*>(hdr + 1);
-    batch_kernel<TW, SPEC><<<blocks, threads, 0, s>>>(hdr, jobs, q, chunk, err);
+    const size_t smem = batch_needs_stacks(SPEC) ? (size_t)2 * STACK_DEPTH * 4 * threads : 0;
+    if (smem > 48 * 1024) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(batch_kernel<TW, SPEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    batch_kernel<TW, SPEC><<<blocks, threads, smem, s>>>(hdr, jobs, q, chunk, err);
     return cudaGetLastError();
 }
 
@@ -1256,16 +1264,25 @@ cudaError_t launch_batch(const void* table, unsigned long long* q, uint32_t* err
     }
 }
 
-// Resident blocks per SM of the generic kernel (the most demanding of the
-// forms, so the specialised ones fit the same grid).
+// Resident blocks per SM of the generic kernel with its stacks (the most
+// demanding of the forms, so the specialised ones fit the same grid).
 int batch_kernel_blocks_per_sm(uint32_t tile_w, uint32_t threads) {
     int n = 0;
+    const size_t smem = (size_t)2 * STACK_DEPTH * 4 * threads;
     cudaError_t e;
     switch (tile_w) {
-    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<4, XN_BATCH_ANY>, (int)threads, 0); break;
-    case 16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<16, XN_BATCH_ANY>, (int)threads, 0); break;
-    case 32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<32, XN_BATCH_ANY>, (int)threads, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<8, XN_BATCH_ANY>, (int)threads, 0); break;
+    case 4: e = cudaFuncSetAttribute(batch_kernel<4, XN_BATCH_ANY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<4, XN_BATCH_ANY>, (int)threads, smem);
+        break;
+    case 16: e = cudaFuncSetAttribute(batch_kernel<16, XN_BATCH_ANY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<16, XN_BATCH_ANY>, (int)threads, smem);
+        break;
+    case 32: e = cudaFuncSetAttribute(batch_kernel<32, XN_BATCH_ANY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<32, XN_BATCH_ANY>, (int)threads, smem);
+        break;
+    default: e = cudaFuncSetAttribute(batch_kernel<8, XN_BATCH_ANY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<8, XN_BATCH_ANY>, (int)threads, smem);
+        break;
     }
     return e == cudaSuccess ? n : 0;
 }

@@ -17,7 +17,8 @@ enum {
     XN_TRAV_ESVO = 2,
     XN_TRAV_SVO_DF = 3,
     XN_TRAV_SVO_ROPE = 4,
-    XN_TRAV_SVO_DF_MASKED = 5  // svo-df on an octree with consistent depth fields (render.cu)
+    XN_TRAV_SVO_DF_MASKED = 5,  // svo-df on an octree with consistent depth fields (render.cu)
+    XN_TRAV_SVO_NAIVE_ROOT = 6  // svo-naive with every find from the root
 };
 
 // Everything one traversal launch needs; built by the C-ABI layer from an
@@ -45,8 +46,8 @@ struct RenderLaunch {
     const uint32_t* inner_depth;
     const uint32_t* leaves;
     int depth_consistent;         // every internal node's depth field = its depth in the tree
-    int esvo_shared_stack;        // esvo with its stack in shared memory
-    int dda_ahead;                // texture DDA: cells fetched ahead of the accumulation (1 or 2)
+    int shared_stacks;            // esvo and masked svo-df with their stacks in shared memory
+    int naive_resume;             // svo-naive's find resumes from the previous step's path
     // outputs (device pointers)
     void* d_rgba;
     float* d_emission;
