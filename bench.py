@@ -265,6 +265,7 @@ def measure_batched(ctx, xg, args):
     batched_ms = timed(lambda: graph.launch(jobs, len(specs)))
     same = all(torch.equal(a, b) for a, b in zip(plain_out, bufs[:: max(1, len(bufs) // 8)]))
     graph.close()
+    small = batched_small_frames(ctx, xg, vol, timed, args)
     vol.release()
     return {
         "workload": f"{n}^3 gas field, rope octree, esvo+svo-rope, {len(cams)} Fibonacci-sphere cameras at 1.8x, "
@@ -273,8 +274,40 @@ def measure_batched(ctx, xg, args):
         "plain_ms": round(plain_ms, 3), "batched_ms": round(batched_ms, 3),
         "plain_mrays_s": round(rays / (plain_ms * 1e3), 1), "batched_mrays_s": round(rays / (batched_ms * 1e3), 1),
         "speedup": round(plain_ms / batched_ms, 3), "identical_images": bool(same), "launch_shape": best.as_dict(),
+        "small_frames": small,
         "dda_4k": dda4k,
     }
+
+
+def batched_small_frames(ctx, xg, vol, timed, args):
+    """The same octree and traversals at 256x256 from 256 cameras: frames too
+    small to fill the GPU one launch at a time, the case batching is for."""
+    import torch
+    from xenodon_gb300 import cameras
+    w = h = 256
+    cams = cameras.fibonacci_sphere(4 * args.batched_cameras, np.array([0.5, 0.5, 0.5]), 1.8,
+                                    cameras.forward_length_for_vfov(45.0, w, h))
+    params = xg.make_params(w, h, EMISSION)
+    specs = [(vol, t, xg.make_camera(*c), params) for t in ("esvo", "svo-rope") for c in cams]
+    bufs = [torch.empty((h, w), dtype=torch.int32, device="cuda") for _ in specs]
+    sptr = torch.cuda.current_stream().cuda_stream
+
+    def plain():
+        for (v, t, c, p), b in zip(specs, bufs):
+            ctx.render_device(v, t, c, p, b.data_ptr(), None, None, sptr)
+
+    plain_ms = timed(plain)
+    keep = [b.clone() for b in bufs[::16]]
+    jobs = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs, bufs))
+    best, _ = ctx.autotune_batch(jobs, len(specs), sptr)
+    for b in bufs:
+        b.fill_(-1)
+    batched_ms = timed(lambda: ctx.render_batch(jobs, len(specs), best, sptr))
+    same = all(torch.equal(a, b) for a, b in zip(keep, bufs[::16]))
+    rays = w * h * len(specs)
+    return {"frames": len(specs), "resolution": [w, h], "plain_mrays_s": round(rays / (plain_ms * 1e3), 1),
+            "batched_mrays_s": round(rays / (batched_ms * 1e3), 1), "speedup": round(plain_ms / batched_ms, 3),
+            "identical_images": bool(same), "launch_shape": best.as_dict()}
 
 
 def measure_dda_4k(ctx, xg, g, n, vol=None):

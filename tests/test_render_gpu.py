@@ -282,13 +282,13 @@ def test_parity_empty_volume_and_degenerate_regions(ctx, trav):
 @pytest.mark.parametrize("trav", ["esvo", "svo-df"])
 @pytest.mark.parametrize("cam", ["oblique", "inside", "grazing"])
 def test_stacks_in_shared_memory_equal_local(ctx, blob_volumes, monkeypatch, trav, cam):
-    # esvo and the masked svo-df keep their stacks in shared memory by
-    # default; XN_STACKS=local selects the local-memory form: same bits,
-    # same word counts
+    # XN_STACKS=shared puts the esvo and masked svo-df stacks in shared
+    # memory, XN_STACKS=local in local memory: same bits, same word counts
     import xenodon_gb300 as xg
     _, nodes, side = blob_volumes
     vol = ctx.upload_svo(nodes, side)
     p, v = _params_pair(xg, 83, 61)
+    monkeypatch.setenv("XN_STACKS", "shared")
     shared, _ = check_parity(ctx, trav, CAMS[cam], p, v, nodes=nodes, vol=vol, label=f"{trav}-shared/{cam}")
     _, em_s, loads_s = _gpu_counts(ctx, vol, trav, xg.make_camera(*CAMS[cam]), p)
     monkeypatch.setenv("XN_STACKS", "local")

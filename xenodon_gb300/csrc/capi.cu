@@ -470,9 +470,12 @@ int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_p
         L.depth_consistent = v->depth_consistent;
         if (traversal == XN_TRAV_SVO_ROPE && v->layout == XN_LAYOUT_COMPACT && !v->rinner)
             return fail(XN_ERR_ARG, "svo-rope: the octree was built lean, without rope records");
-        // esvo's and svo-df's stacks in shared memory unless XN_STACKS=local
+        // traversal stacks: esvo's in shared memory, svo-df's in local memory
+        // (measured fastest); XN_STACKS=local / shared puts both in one place
         const char* es = std::getenv("XN_STACKS");
-        L.shared_stacks = !(es && std::strcmp(es, "local") == 0);
+        const bool all_local = es && std::strcmp(es, "local") == 0;
+        const bool all_shared = es && std::strcmp(es, "shared") == 0;
+        L.shared_stacks = all_local ? 0 : (all_shared || traversal == XN_TRAV_ESVO) ? 1 : 0;
         // svo-naive's find resumes from the last path unless XN_NAIVE_FIND=root
         const char* nf = std::getenv("XN_NAIVE_FIND");
         L.naive_resume = !(nf && std::strcmp(nf, "root") == 0);
