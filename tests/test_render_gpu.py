@@ -313,3 +313,22 @@ def test_naive_resumed_find_equals_root_descent(ctx, blob_volumes, monkeypatch, 
     _, em_0, loads_0 = _gpu_counts(ctx, vol, "svo-naive", xg.make_camera(*CAMS[cam]), p)
     assert np.array_equal(resumed, root)
     assert np.array_equal(em_r, em_0) and np.array_equal(loads_r, loads_0)
+
+
+@pytest.mark.parametrize("size", [(96, 64), (37, 23), (1, 1), (130, 7)])
+@pytest.mark.parametrize("cam", ["oblique", "inside", "grazing", "front"])
+def test_df_walked_by_the_warp_equals_one_ray_per_thread(ctx, blob_volumes, monkeypatch, size, cam):
+    # XN_DF_PACKET=1: the warp walks the union of its lanes' hit children;
+    # each ray's bits and word count must be those of its own traversal
+    import xenodon_gb300 as xg
+    _, nodes, side = blob_volumes
+    vol = ctx.upload_svo(nodes, side)
+    p, v = _params_pair(xg, *size)
+    monkeypatch.setenv("XN_DF_PACKET", "1")
+    packet, _ = check_parity(ctx, "svo-df", CAMS[cam], p, v, nodes=nodes, vol=vol, label=f"df-packet/{cam}")
+    _, em_p, loads_p = _gpu_counts(ctx, vol, "svo-df", xg.make_camera(*CAMS[cam]), p)
+    monkeypatch.setenv("XN_DF_PACKET", "0")
+    plain, _, _ = ctx.render(vol, "svo-df", xg.make_camera(*CAMS[cam]), p)
+    _, em_0, loads_0 = _gpu_counts(ctx, vol, "svo-df", xg.make_camera(*CAMS[cam]), p)
+    assert np.array_equal(packet, plain)
+    assert np.array_equal(em_p, em_0) and np.array_equal(loads_p, loads_0)

@@ -896,6 +896,127 @@ __global__ void __launch_bounds__(BLOCK_THREADS) svo_kernel(Frame f, Acc a, Outp
     write_outputs(f, o, ix, iy, color, loads, err);
 }
 
+// svo-df, masked form, walked by the whole warp at once.  Each lane has its
+// own ray and its own hit masks; the warp visits the union of the lanes' hit
+// children in index order, descending depth first as the reference does.  A
+// lane that hits a child does exactly what its own masked traversal would do
+// there (accumulate a leaf, or descend and take the child's hit mask), a lane
+// that does not sits out that child's subtree with empty masks.  Restricted
+// to one lane, the union walk visits that lane's hit children in the same
+// order with the same arithmetic, so every ray's result (and its word count)
+// is the one-ray-per-thread result, while the control flow, the node loads
+// (one address per warp) and the pops are shared by the warp.
+//   w_node / w_state: the warp's stack (node, union of remaining masks |
+//   depth << 8); l_mask: each lane's remaining mask per stack entry.
+template <bool COUNT, class Acc>
+__device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t& loads, uint32_t& err,
+                              uint32_t* w_node, uint32_t* w_state, uint8_t* l_mask) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const V3 rrd = vs(1.0f) / rd;
+    const V3 bias = rrd * ro;
+    int sp = 0;
+    uint32_t node = a.root();
+    uint32_t depth = 0;
+    V3 origin = vs(0.0f);
+    float side = 0.5f;
+    V3 total = vs(0.0f);
+    ChildSlabs slabs = child_slabs(origin, side, rrd, bias);
+    uint32_t own = active ? hit_mask(slabs) : 0u;
+    if (COUNT && active) loads += 8;
+    uint32_t uni = __reduce_or_sync(0xFFFFFFFFu, own);
+    uint32_t iter = 0;
+    for (;;) {
+        if (++iter > SVO_MAX_ITER) {
+            if (active) err |= 1u;
+            break;
+        }
+        if (uni == 0) {
+            // every lane is done with this node: pop (the reference reads the
+            // parent's depth; masked svo-df takes it from the stack)
+            --sp;
+            if (sp < 0) break;
+            node = w_node[sp];
+            const uint32_t st = w_state[sp];
+            uni = st & 0xFFu;
+            depth = st >> 8;
+            own = l_mask[sp * 32 + lane];
+            float s2, inv;
+            bool ex;
+            if (depth <= 124u) {
+                s2 = __uint_as_float((127u - depth) << 23);
+                inv = __uint_as_float((127u + depth) << 23);
+                side = s2 * 0.5f;
+                ex = true;
+            } else {
+                side = ldexpf(1.0f, -(int)(depth > 1000u ? 1000u : depth)) * 0.5f;
+                s2 = side * 2.0f;
+                inv = __frcp_rn(s2);
+                ex = pow2_with_normal_reciprocal(s2);
+            }
+            origin = origin - v3(gl_mod_pow2(origin.x, s2, inv, ex), gl_mod_pow2(origin.y, s2, inv, ex),
+                                 gl_mod_pow2(origin.z, s2, inv, ex));
+            slabs = child_slabs(origin, side, rrd, bias);
+            continue;
+        }
+        const uint32_t k = __ffs(uni) - 1;
+        uni &= uni - 1;
+        const bool mine = (own >> k) & 1u;
+        own &= ~(1u << k);
+        const uint32_t child = a.child(node, k);
+        if (COUNT && mine) ++loads;
+        if (a.is_leaf(child)) {
+            if (mine) {
+                float t0, t1;
+                child_span(slabs, k, t0, t1);
+                const V3 color = unpack_rgb(a.color(child));
+                if (COUNT) ++loads;
+                total = total + color * (t1 - fmaxf(t0, 0.0f));
+            }
+            continue;
+        }
+        // descend into child k (lanes that miss it sit out its subtree)
+        if (uni != 0) {
+            if (sp >= STACK_DEPTH) {
+                if (active) err |= 2u;
+                break;
+            }
+            if (lane == 0) {
+                w_node[sp] = node;
+                w_state[sp] = uni | (depth << 8);
+            }
+            l_mask[sp * 32 + lane] = (uint8_t)own;
+            ++sp;
+        }
+        if (COUNT && mine && k != 7) ++loads;  // the pop back to this node reads its depth
+        origin = v3(origin.x + ((k & 4u) ? side : 0.0f), origin.y + ((k & 2u) ? side : 0.0f),
+                    origin.z + ((k & 1u) ? side : 0.0f));
+        node = child;
+        ++depth;
+        side *= 0.5f;
+        slabs = child_slabs(origin, side, rrd, bias);
+        own = mine ? hit_mask(slabs) : 0u;
+        if (COUNT && mine) loads += 8;
+        uni = __reduce_or_sync(0xFFFFFFFFu, own);
+        __syncwarp();
+    }
+    return total;
+}
+
+template <bool COUNT, class Acc>
+__global__ void __launch_bounds__(BLOCK_THREADS) df_packet_kernel(Frame f, Acc a, Outputs o) {
+    __shared__ uint32_t s_node[(BLOCK_THREADS / 32) * STACK_DEPTH];
+    __shared__ uint32_t s_state[(BLOCK_THREADS / 32) * STACK_DEPTH];
+    __shared__ uint8_t s_mask[(BLOCK_THREADS / 32) * STACK_DEPTH * 32];
+    const uint32_t warp = threadIdx.x >> 5;
+    uint32_t ix, iy;
+    const bool active = pixel_of_thread(f, ix, iy);
+    const V3 rd = primary_ray(f, active ? ix : 0u, active ? iy : 0u);
+    uint32_t loads = 0, err = 0;
+    const V3 total = trace_df_packet<COUNT>(a, f.translation, rd, active, loads, err, s_node + warp * STACK_DEPTH,
+                                            s_state + warp * STACK_DEPTH, s_mask + warp * STACK_DEPTH * 32);
+    if (active) write_outputs(f, o, ix, iy, total * voxel_emission_coeff(f, rd), loads, err);
+}
+
 // esvo and the masked svo-df with their stacks in shared memory (23.5 KB per
 // block of 128).
 template <int TRAV, bool COUNT, class Acc>
@@ -983,6 +1104,10 @@ cudaError_t launch_render(const RenderLaunch& L, cudaStream_t stream) {
             if (count) shared_stack_kernel<XN_TRAV_ESVO, true><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
             else shared_stack_kernel<XN_TRAV_ESVO, false><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
         }
+    } else if (L.traversal == XN_TRAV_SVO_DF && L.df_packet && L.layout == XN_LAYOUT_COMPACT && L.depth_consistent) {
+        const CompactNodes acc{L.inner, L.inner_depth};
+        if (count) df_packet_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
+        else df_packet_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
     } else if (L.traversal == XN_TRAV_SVO_DF && L.shared_stacks && L.layout == XN_LAYOUT_COMPACT &&
                L.depth_consistent) {
         const CompactNodes acc{L.inner, L.inner_depth};

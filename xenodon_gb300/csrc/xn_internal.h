@@ -48,6 +48,7 @@ struct RenderLaunch {
     int depth_consistent;         // every internal node's depth field = its depth in the tree
     int shared_stacks;            // esvo and masked svo-df with their stacks in shared memory
     int naive_resume;             // svo-naive's find resumes from the previous step's path
+    int df_packet;                // masked svo-df walked by the whole warp (df_packet_kernel)
     // outputs (device pointers)
     void* d_rgba;
     float* d_emission;
