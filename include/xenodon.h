@@ -178,7 +178,8 @@ typedef struct {
     uint32_t tile_width;    /* warp tile width in pixels: 4, 8, 16 or 32 (height = 32/width) */
     uint32_t block_threads; /* threads per block: a multiple of 32, at most 1024 */
     uint32_t blocks_per_sm; /* resident blocks per SM; 0 = as many as fit */
-    uint32_t chunk;         /* warp tiles a warp takes per pop of the work queue, >= 1 */
+    uint32_t chunk;         /* warp tiles a warp takes per pop of the work queue; 0: no queue, a grid of
+                               one warp per tile (batch graphs use 1 instead) */
 } xn_batch_config;
 
 /* Renders n_jobs frames of any mix of volumes, traversals and resolutions in

@@ -65,7 +65,8 @@ def _batch_buffers(specs):
             for _, _, _, p in specs]
 
 
-@pytest.mark.parametrize("tile,threads,chunk", [(8, 128, 1), (4, 64, 3), (16, 256, 2), (32, 96, 1), (8, 1024, 7)])
+@pytest.mark.parametrize("tile,threads,chunk", [(8, 128, 1), (4, 64, 3), (16, 256, 2), (32, 96, 1), (8, 1024, 7),
+                                                (8, 128, 0), (4, 256, 0), (32, 1024, 0)])
 def test_batch_equals_single_frame_renders(ctx, scene, tile, threads, chunk):
     import torch
     xg, _ = scene
@@ -124,7 +125,7 @@ def test_batch_rejects_bad_shapes_and_jobs(ctx, scene):
     specs = _specs(scene)[:1]
     bufs = _batch_buffers(specs)
     jobs = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs, bufs))
-    for cfg in (xg.BatchConfig(6, 128, 0, 1), xg.BatchConfig(8, 100, 0, 1), xg.BatchConfig(8, 128, 0, 0)):
+    for cfg in (xg.BatchConfig(6, 128, 0, 1), xg.BatchConfig(8, 100, 0, 1), xg.BatchConfig(8, 0, 0, 1)):
         with pytest.raises(xg.XenodonError) as e:
             ctx.render_batch(jobs, 1, cfg)
         assert e.value.code == xg.XN_ERR_ARG
@@ -147,7 +148,7 @@ def test_single_traversal_batches_use_the_inlined_form(ctx, scene, monkeypatch, 
     stream = torch.cuda.current_stream().cuda_stream
     for generic in ("0", "1"):
         monkeypatch.setenv("XN_BATCH_GENERIC", generic)
-        for cfg in (xg.BatchConfig(8, 128, 0, 1), xg.BatchConfig(4, 64, 0, 3)):
+        for cfg in (xg.BatchConfig(8, 128, 0, 1), xg.BatchConfig(4, 64, 0, 3), xg.BatchConfig(8, 256, 0, 0)):
             bufs = _batch_buffers(specs)
             jobs = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs, bufs))
             ctx.render_batch(jobs, len(specs), cfg, stream)

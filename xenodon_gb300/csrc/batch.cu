@@ -28,7 +28,7 @@ int check_config(const xn_batch_config& c) {
         return fail(XN_ERR_ARG, "batch: tile_width must be 4, 8, 16 or 32");
     if (c.block_threads == 0 || c.block_threads % 32 || c.block_threads > 1024)
         return fail(XN_ERR_ARG, "batch: block_threads must be a multiple of 32 up to 1024");
-    if (c.chunk == 0) return fail(XN_ERR_ARG, "batch: chunk must be >= 1");
+
     return XN_OK;
 }
 
@@ -116,9 +116,19 @@ int render_batch_locked(Ctx* c, const xn_job* jobs, int n, const xn_batch_config
     e = cudaMemcpyAsync(d, c->batch_host, bytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaEventRecord(c->batch_copied, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(queue, 0, 8, s);
+    const uint64_t total_tiles = static_cast<const BatchHeader*>(c->batch_host)->total_tiles;
+    const uint32_t warps = cfg.block_threads / 32;
+    const uint64_t grid = cfg.chunk ? resident_blocks(c, cfg) : (total_tiles + warps - 1) / warps;
+    if (grid == 0) {
+        cudaFreeAsync(d, s);
+        return XN_OK;
+    }
+    if (grid > 0x7FFFFFFFull) {
+        cudaFreeAsync(d, s);
+        return fail(XN_ERR_ARG, "xn_render_batch: too many tiles for one grid; use a queue chunk >= 1");
+    }
     if (e == cudaSuccess)
-        e = launch_batch(d, queue, c->d_err, cfg.tile_width, cfg.block_threads, resident_blocks(c, cfg), cfg.chunk, spec,
-                         s);
+        e = launch_batch(d, queue, c->d_err, cfg.tile_width, cfg.block_threads, (uint32_t)grid, cfg.chunk, spec, s);
     const cudaError_t ef = cudaFreeAsync(d, s);
     if (e == cudaSuccess) e = ef;
     return e == cudaSuccess ? XN_OK : cuda_fail(e, "xn_render_batch");
@@ -166,7 +176,7 @@ XN_API int xn_autotune_batch(xn_ctx* h, const xn_job* jobs, int n, void* stream,
         return fail(XN_ERR_CUDA, "xn_autotune_batch: events");
     const uint32_t tiles[] = {4, 8, 16, 32};
     const uint32_t threads[] = {64, 128, 256};
-    const uint32_t chunks[] = {1, 2, 4};
+    const uint32_t chunks[] = {0, 1, 2, 4};  // 0: one warp per tile over a full grid, no queue
     xn_batch_config winner = default_config();
     float winner_ms = 3.4e38f;
     for (uint32_t tw : tiles)
@@ -254,6 +264,7 @@ XN_API int xn_batch_graph_create(xn_ctx* h, int capacity, const xn_batch_config*
     g->ctx = c;
     g->stream = static_cast<cudaStream_t>(stream);
     g->cfg = cfg ? *cfg : default_config();
+    if (g->cfg.chunk == 0) g->cfg.chunk = 1;  // the tile count changes per replay: graphs use the queue form
     g->capacity = capacity;
     g->table_bytes = sizeof(BatchHeader) + (uint64_t)capacity * sizeof(BatchJob);
     if ((r = check_config(g->cfg))) {

@@ -1346,6 +1346,37 @@ __global__ void __launch_bounds__(1024) batch_kernel(const BatchHeader* hdr, con
     if (err) atomicOr(err_word, err);
 }
 
+// The queue-less form of the batch kernel (chunk 0): a grid with one warp
+// per tile of every job, in tile order; the hardware block scheduler
+// balances the load.  Same per-pixel arithmetic as batch_kernel.
+template <int TW, int SPEC>
+__global__ void __launch_bounds__(1024) batch_grid_kernel(const BatchHeader* hdr, const BatchJob* jobs,
+                                                          uint32_t* err_word) {
+    constexpr int TH = 32 / TW;
+    extern __shared__ uint32_t batch_stacks[];
+    SharedStacks stk{batch_stacks + threadIdx.x, batch_stacks + STACK_DEPTH * blockDim.x + threadIdx.x, blockDim.x};
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned long long t =
+        (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (t >= hdr->total_tiles) return;
+    uint32_t lo = 0, hi = hdr->n_jobs;  // last job whose first tile is <= t
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (jobs[mid].tile_begin <= t) lo = mid;
+        else hi = mid;
+    }
+    const BatchJob& J = jobs[lo];
+    const unsigned long long local = t - J.tile_begin;
+    const uint32_t ty = (uint32_t)(local / J.tiles_x);
+    const uint32_t tx = (uint32_t)(local - (unsigned long long)ty * J.tiles_x);
+    const uint32_t ix = tx * TW + lane % TW, iy = ty * TH + lane / TW;
+    if (ix >= J.out_w || iy >= J.out_h) return;
+    uint32_t err = 0;
+    const uint32_t px = render_job_pixel_spec<SPEC>(J, ix, iy, err, &stk);
+    static_cast<uint32_t*>(J.rgba)[(uint64_t)iy * J.out_w + ix] = px;
+    if (err) atomicOr(err_word, err);
+}
+
 constexpr bool batch_needs_stacks(int spec) {
     return spec == XN_BATCH_ANY || spec == XN_BATCH_ESVO || spec == XN_BATCH_DF;
 }
@@ -1356,6 +1387,16 @@ static cudaError_t launch_batch_tws(const void* table, unsigned long long* q, ui
     const BatchHeader* hdr = static_cast<const BatchHeader*>(table);
     const BatchJob* jobs = reinterpret_cast<const BatchJob*>(hdr + 1);
     const size_t smem = batch_needs_stacks(SPEC) ? (size_t)2 * STACK_DEPTH * 4 * threads : 0;
+    if (chunk == 0) {
+        // queue-less form: one warp per tile; `blocks` is the grid for all tiles
+        if (smem > 48 * 1024) {
+            const cudaError_t e =
+                cudaFuncSetAttribute(batch_grid_kernel<TW, SPEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        batch_grid_kernel<TW, SPEC><<<blocks, threads, smem, s>>>(hdr, jobs, err);
+        return cudaGetLastError();
+    }
     if (smem > 48 * 1024) {
         const cudaError_t e =
             cudaFuncSetAttribute(batch_kernel<TW, SPEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
