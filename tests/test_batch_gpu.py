@@ -109,7 +109,7 @@ def test_autotune_picks_a_valid_shape_and_is_used(ctx, scene):
     jobs = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs, bufs))
     stream = torch.cuda.current_stream().cuda_stream
     best, ms = ctx.autotune_batch(jobs, len(specs), stream)
-    assert best.tile_width in (4, 8, 16, 32) and best.block_threads % 32 == 0 and best.chunk >= 1 and ms > 0
+    assert best.tile_width in (4, 8, 16, 32) and best.block_threads % 32 == 0 and best.chunk in (0, 1, 2, 4) and ms > 0
     ref = _reference_frames(ctx, specs)
     bufs2 = _batch_buffers(specs)
     jobs2 = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs, bufs2))
