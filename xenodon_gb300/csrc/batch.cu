@@ -56,6 +56,7 @@ int fill_table(Ctx* c, const xn_job* jobs, int n, uint32_t tile_w, void* table, 
         out[i].tile_begin = tiles;
         tiles += (unsigned long long)out[i].tiles_x * out[i].tiles_y;
         const int sp = batch_spec(out[i]);
+        out[i].form = sp;
         if (spec_out) *spec_out = i == 0 ? sp : (*spec_out == sp ? sp : XN_BATCH_ANY);
     }
     h->n_jobs = (uint32_t)n;

@@ -1279,7 +1279,18 @@ template <int SPEC>
 __device__ __forceinline__ uint32_t render_job_pixel_spec(const BatchJob& J, uint32_t ix, uint32_t iy, uint32_t& err,
                                                           SharedStacks* stk) {
     if constexpr (SPEC == XN_BATCH_ANY) {
-        return render_job_pixel(J, ix, iy, err, stk);
+        // a mixed batch: the job's own inlined form, chosen per tile (every
+        // lane of a warp tile has the same job); linear grids, reference
+        // layouts and the literal svo-df go through the generic function
+        switch (J.form) {
+        case XN_BATCH_DDA_TEX_NORM: return render_job_pixel_spec<XN_BATCH_DDA_TEX_NORM>(J, ix, iy, err, stk);
+        case XN_BATCH_DDA_TEX_RAW: return render_job_pixel_spec<XN_BATCH_DDA_TEX_RAW>(J, ix, iy, err, stk);
+        case XN_BATCH_ESVO: return render_job_pixel_spec<XN_BATCH_ESVO>(J, ix, iy, err, stk);
+        case XN_BATCH_NAIVE: return render_job_pixel_spec<XN_BATCH_NAIVE>(J, ix, iy, err, stk);
+        case XN_BATCH_DF: return render_job_pixel_spec<XN_BATCH_DF>(J, ix, iy, err, stk);
+        case XN_BATCH_ROPE: return render_job_pixel_spec<XN_BATCH_ROPE>(J, ix, iy, err, stk);
+        default: return render_job_pixel(J, ix, iy, err, stk);
+        }
     } else {
         const Frame f = frame_of(J);
         const V3 rd = primary_ray(f, ix, iy);

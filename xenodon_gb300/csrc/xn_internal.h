@@ -71,7 +71,7 @@ struct alignas(16) BatchJob {
     uint32_t dim[3];
     int32_t tex_normalized;
     int32_t depth_consistent;
-    int32_t pad0;
+    int32_t form;  // XN_BATCH_* form of this job (batch_spec)
     unsigned long long tex;
     const void* grid;
     const void* nodes;
