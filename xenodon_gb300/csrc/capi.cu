@@ -479,9 +479,9 @@ int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_p
         // svo-naive's find resumes from the last path unless XN_NAIVE_FIND=root
         const char* nf = std::getenv("XN_NAIVE_FIND");
         L.naive_resume = !(nf && std::strcmp(nf, "root") == 0);
-        // masked svo-df walked by the whole warp when XN_DF_PACKET=1
+        // masked svo-df walked by the whole warp unless XN_DF_PACKET=0
         const char* pk = std::getenv("XN_DF_PACKET");
-        L.df_packet = pk ? pk[0] == '1' : 0;
+        L.df_packet = !(pk && pk[0] == '0');
     }
     for (int i = 0; i < 3; ++i) L.dim[i] = v->dim[i];
     return XN_OK;

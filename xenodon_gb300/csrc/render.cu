@@ -908,9 +908,34 @@ __global__ void __launch_bounds__(BLOCK_THREADS) svo_kernel(Frame f, Acc a, Outp
 // (one address per warp) and the pops are shared by the warp.
 //   w_node / w_state: the warp's stack (node, union of remaining masks |
 //   depth << 8); l_mask: each lane's remaining mask per stack entry.
-template <bool COUNT, class Acc>
-__device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t& loads, uint32_t& err,
-                              uint32_t* w_node, uint32_t* w_state, uint8_t* l_mask) {
+// The warp's stacks for trace_df_packet: contiguous per-warp arrays (its own
+// kernel) or, in the batch kernel, carved from the per-thread columns of the
+// shared stacks (warp stack in lanes 0 and 1's first columns, each lane's
+// masks in its own second column), so they never overlap another warp's.
+struct PacketStacksWarp {
+    uint32_t* w_node;
+    uint32_t* w_state;
+    uint8_t* l_mask;
+    uint32_t lane;
+    __device__ __forceinline__ uint32_t& node(int i) { return w_node[i]; }
+    __device__ __forceinline__ uint32_t& state(int i) { return w_state[i]; }
+    __device__ __forceinline__ uint32_t mask(int i) const { return l_mask[i * 32 + lane]; }
+    __device__ __forceinline__ void set_mask(int i, uint32_t m) { l_mask[i * 32 + lane] = (uint8_t)m; }
+};
+
+struct PacketStacksColumns {
+    uint32_t* node0;   // lane 0's first column
+    uint32_t* state0;  // lane 1's first column
+    uint32_t* mine;    // this lane's second column
+    uint32_t stride;
+    __device__ __forceinline__ uint32_t& node(int i) { return node0[i * stride]; }
+    __device__ __forceinline__ uint32_t& state(int i) { return state0[i * stride]; }
+    __device__ __forceinline__ uint32_t mask(int i) const { return mine[i * stride]; }
+    __device__ __forceinline__ void set_mask(int i, uint32_t m) { mine[i * stride] = m; }
+};
+
+template <bool COUNT, class Acc, class PS>
+__device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t& loads, uint32_t& err, PS& ps) {
     const uint32_t lane = threadIdx.x & 31u;
     const V3 rrd = vs(1.0f) / rd;
     const V3 bias = rrd * ro;
@@ -935,11 +960,11 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
             // parent's depth; masked svo-df takes it from the stack)
             --sp;
             if (sp < 0) break;
-            node = w_node[sp];
-            const uint32_t st = w_state[sp];
+            node = ps.node(sp);
+            const uint32_t st = ps.state(sp);
             uni = st & 0xFFu;
             depth = st >> 8;
-            own = l_mask[sp * 32 + lane];
+            own = ps.mask(sp);
             float s2, inv;
             bool ex;
             if (depth <= 124u) {
@@ -981,10 +1006,10 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
                 break;
             }
             if (lane == 0) {
-                w_node[sp] = node;
-                w_state[sp] = uni | (depth << 8);
+                ps.node(sp) = node;
+                ps.state(sp) = uni | (depth << 8);
             }
-            l_mask[sp * 32 + lane] = (uint8_t)own;
+            ps.set_mask(sp, own);
             ++sp;
         }
         if (COUNT && mine && k != 7) ++loads;  // the pop back to this node reads its depth
@@ -1012,8 +1037,9 @@ __global__ void __launch_bounds__(BLOCK_THREADS) df_packet_kernel(Frame f, Acc a
     const bool active = pixel_of_thread(f, ix, iy);
     const V3 rd = primary_ray(f, active ? ix : 0u, active ? iy : 0u);
     uint32_t loads = 0, err = 0;
-    const V3 total = trace_df_packet<COUNT>(a, f.translation, rd, active, loads, err, s_node + warp * STACK_DEPTH,
-                                            s_state + warp * STACK_DEPTH, s_mask + warp * STACK_DEPTH * 32);
+    PacketStacksWarp ps{s_node + warp * STACK_DEPTH, s_state + warp * STACK_DEPTH, s_mask + warp * STACK_DEPTH * 32,
+                        threadIdx.x & 31u};
+    const V3 total = trace_df_packet<COUNT>(a, f.translation, rd, active, loads, err, ps);
     if (active) write_outputs(f, o, ix, iy, total * voxel_emission_coeff(f, rd), loads, err);
 }
 
@@ -1275,20 +1301,35 @@ __device__ __noinline__ uint32_t render_job_pixel(const BatchJob& J, uint32_t ix
 
 // One pixel of a job whose traversal and layout the whole batch shares
 // (BatchSpec): that traversal inlined, the arithmetic of render_job_pixel.
+// Called by every lane of a warp tile (active: the pixel is in the job's
+// output); the svo-df form walks the tree with the whole warp.
 template <int SPEC>
-__device__ __forceinline__ uint32_t render_job_pixel_spec(const BatchJob& J, uint32_t ix, uint32_t iy, uint32_t& err,
-                                                          SharedStacks* stk) {
+__device__ __forceinline__ uint32_t render_job_pixel_spec(const BatchJob& J, uint32_t ix, uint32_t iy, bool active,
+                                                          uint32_t& err, SharedStacks* stk) {
+    if constexpr (SPEC == XN_BATCH_DF) {
+        const Frame f = frame_of(J);
+        const V3 rd = primary_ray(f, active ? ix : 0u, active ? iy : 0u);
+        const uint32_t lane = threadIdx.x & 31u;
+        PacketStacksColumns ps{stk->a - lane, stk->a - lane + 1, stk->b, stk->stride};
+        uint32_t loads = 0;
+        const V3 total = trace_df_packet<false>(CompactNodes{J.inner, J.inner_depth}, f.translation, rd, active,
+                                                loads, err, ps);
+        return pack_rgba(total * voxel_emission_coeff(f, rd));
+    }
+    if constexpr (SPEC == XN_BATCH_ANY) {
+        if (J.form == XN_BATCH_DF) return render_job_pixel_spec<XN_BATCH_DF>(J, ix, iy, active, err, stk);
+    }
+    if (!active) return 0u;
     if constexpr (SPEC == XN_BATCH_ANY) {
         // a mixed batch: the job's own inlined form, chosen per tile (every
         // lane of a warp tile has the same job); linear grids, reference
         // layouts and the literal svo-df go through the generic function
         switch (J.form) {
-        case XN_BATCH_DDA_TEX_NORM: return render_job_pixel_spec<XN_BATCH_DDA_TEX_NORM>(J, ix, iy, err, stk);
-        case XN_BATCH_DDA_TEX_RAW: return render_job_pixel_spec<XN_BATCH_DDA_TEX_RAW>(J, ix, iy, err, stk);
-        case XN_BATCH_ESVO: return render_job_pixel_spec<XN_BATCH_ESVO>(J, ix, iy, err, stk);
-        case XN_BATCH_NAIVE: return render_job_pixel_spec<XN_BATCH_NAIVE>(J, ix, iy, err, stk);
-        case XN_BATCH_DF: return render_job_pixel_spec<XN_BATCH_DF>(J, ix, iy, err, stk);
-        case XN_BATCH_ROPE: return render_job_pixel_spec<XN_BATCH_ROPE>(J, ix, iy, err, stk);
+        case XN_BATCH_DDA_TEX_NORM: return render_job_pixel_spec<XN_BATCH_DDA_TEX_NORM>(J, ix, iy, true, err, stk);
+        case XN_BATCH_DDA_TEX_RAW: return render_job_pixel_spec<XN_BATCH_DDA_TEX_RAW>(J, ix, iy, true, err, stk);
+        case XN_BATCH_ESVO: return render_job_pixel_spec<XN_BATCH_ESVO>(J, ix, iy, true, err, stk);
+        case XN_BATCH_NAIVE: return render_job_pixel_spec<XN_BATCH_NAIVE>(J, ix, iy, true, err, stk);
+        case XN_BATCH_ROPE: return render_job_pixel_spec<XN_BATCH_ROPE>(J, ix, iy, true, err, stk);
         default: return render_job_pixel(J, ix, iy, err, stk);
         }
     } else {
@@ -1318,8 +1359,14 @@ __device__ __forceinline__ uint32_t render_job_pixel_spec(const BatchJob& J, uin
     }
 }
 
+// The texture-DDA forms are held to 32 registers (two blocks of 1024 per SM):
+// DDA hides texture latency with resident warps.
+constexpr int batch_min_blocks(int spec) {
+    return spec == XN_BATCH_DDA_TEX_NORM || spec == XN_BATCH_DDA_TEX_RAW ? 2 : 1;
+}
+
 template <int TW, int SPEC>
-__global__ void __launch_bounds__(1024) batch_kernel(const BatchHeader* hdr, const BatchJob* jobs,
+__global__ void __launch_bounds__(1024, batch_min_blocks(SPEC)) batch_kernel(const BatchHeader* hdr, const BatchJob* jobs,
                                                      unsigned long long* queue, uint32_t chunk, uint32_t* err_word) {
     constexpr int TH = 32 / TW;
     // esvo and svo-df stacks: two columns per thread in dynamic shared memory
@@ -1348,10 +1395,9 @@ __global__ void __launch_bounds__(1024) batch_kernel(const BatchHeader* hdr, con
             const uint32_t ty = (uint32_t)(local / J.tiles_x);
             const uint32_t tx = (uint32_t)(local - (unsigned long long)ty * J.tiles_x);
             const uint32_t ix = tx * TW + lane % TW, iy = ty * TH + lane / TW;
-            if (ix < J.out_w && iy < J.out_h) {
-                const uint32_t px = render_job_pixel_spec<SPEC>(J, ix, iy, err, &stk);
-                static_cast<uint32_t*>(J.rgba)[(uint64_t)iy * J.out_w + ix] = px;
-            }
+            const bool active = ix < J.out_w && iy < J.out_h;
+            const uint32_t px = render_job_pixel_spec<SPEC>(J, ix, iy, active, err, &stk);
+            if (active) static_cast<uint32_t*>(J.rgba)[(uint64_t)iy * J.out_w + ix] = px;
         }
     }
     if (err) atomicOr(err_word, err);
@@ -1361,7 +1407,7 @@ __global__ void __launch_bounds__(1024) batch_kernel(const BatchHeader* hdr, con
 // per tile of every job, in tile order; the hardware block scheduler
 // balances the load.  Same per-pixel arithmetic as batch_kernel.
 template <int TW, int SPEC>
-__global__ void __launch_bounds__(1024) batch_grid_kernel(const BatchHeader* hdr, const BatchJob* jobs,
+__global__ void __launch_bounds__(1024, batch_min_blocks(SPEC)) batch_grid_kernel(const BatchHeader* hdr, const BatchJob* jobs,
                                                           uint32_t* err_word) {
     constexpr int TH = 32 / TW;
     extern __shared__ uint32_t batch_stacks[];
@@ -1381,10 +1427,10 @@ __global__ void __launch_bounds__(1024) batch_grid_kernel(const BatchHeader* hdr
     const uint32_t ty = (uint32_t)(local / J.tiles_x);
     const uint32_t tx = (uint32_t)(local - (unsigned long long)ty * J.tiles_x);
     const uint32_t ix = tx * TW + lane % TW, iy = ty * TH + lane / TW;
-    if (ix >= J.out_w || iy >= J.out_h) return;
+    const bool active = ix < J.out_w && iy < J.out_h;
     uint32_t err = 0;
-    const uint32_t px = render_job_pixel_spec<SPEC>(J, ix, iy, err, &stk);
-    static_cast<uint32_t*>(J.rgba)[(uint64_t)iy * J.out_w + ix] = px;
+    const uint32_t px = render_job_pixel_spec<SPEC>(J, ix, iy, active, err, &stk);
+    if (active) static_cast<uint32_t*>(J.rgba)[(uint64_t)iy * J.out_w + ix] = px;
     if (err) atomicOr(err_word, err);
 }
 
