@@ -232,6 +232,10 @@ XN_API int xn_server_add_svo(xn_server* server, uint32_t volume_id, const uint32
                              uint64_t side);
 /* Queue a frame; out_rgba (width*height*4 bytes of host memory) must stay
  * valid until xn_server_wait returns for the ticket. */
+/* A volume already resident in the server's context (built on the device,
+ * loaded from an XNDN-SVC file, ...): the caller keeps owning it, the server
+ * counts it against the budget and never evicts or releases it. */
+XN_API int xn_server_add_volume(xn_server* server, uint32_t volume_id, xn_volume* volume);
 XN_API int xn_server_submit(xn_server* server, uint32_t volume_id, int traversal, const xn_camera* cam,
                             const xn_params* params, uint8_t* out_rgba, uint64_t* ticket);
 /* Wait for a ticket (timeout_s < 0: no limit); releases the ticket. */

@@ -114,3 +114,35 @@ def test_server_rejects_bad_requests(ctx, volumes_data):
         t = server.submit(1, "dda", cam, xg.make_params(8, 8))
         with pytest.raises(xg.XenodonError):
             server.wait(t, timeout=30)
+
+
+def test_resident_volumes_are_served_and_never_evicted(ctx, volumes_data):
+    # xn_server_add_volume: a volume built on the device (no host copy) is
+    # served like the others, counted in the budget, and left to its owner
+    import torch
+    import xenodon_gb300 as xg
+    from xenodon_gb300 import volumes
+    g = volumes.blobs(48, seed=21)
+    d = torch.from_numpy(g).cuda()
+    lean, _ = ctx.build_svo_volume(d.data_ptr(), (48, 48, 48), "sparse", lean=True)
+    size = lean.info()["device_bytes"]
+    cam = xg.make_camera((0.35, -0.2, -0.91), (0.0, 0.976, -0.215), (0.2, 0.8, 2.0))
+    p = xg.make_params(40, 30, 10.0)
+    alone, _, _ = ctx.render(lean, "esvo", cam, p)
+    kind, g0 = volumes_data[1]
+    budget = size + g0.nbytes + (1 << 20)
+    with xg.Server(ctx, hbm_budget=budget, max_batch_jobs=4) as server:
+        server.add_volume(7, lean)
+        server.add_grid(1, g0)
+        for _ in range(3):  # alternate: the grid is uploaded, the resident volume never leaves
+            t = server.submit(7, "esvo", cam, p)
+            assert np.array_equal(server.wait(t, timeout=60)[0], alone)
+            t = server.submit(1, "dda", cam, p)
+            server.wait(t, timeout=60)
+        st = server.stats()
+        assert st["hbm_used"] <= budget
+        with pytest.raises(xg.XenodonError):
+            server.add_volume(8, lean)  # over the budget with the grid resident
+    # the owner's volume is still usable after the server is gone
+    again, _, _ = ctx.render(lean, "esvo", cam, p)
+    assert np.array_equal(again, alone)

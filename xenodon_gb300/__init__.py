@@ -35,7 +35,7 @@ EXPORTS = (
     "xn_render", "xn_render_device", "xn_ray_errors", "xn_build_svo", "xn_build_svo_static", "xn_free",
     "xn_render_batch", "xn_autotune_batch", "xn_batch_graph_create", "xn_batch_graph_launch",
     "xn_batch_graph_destroy", "xn_server_create", "xn_server_destroy", "xn_server_add_grid",
-    "xn_server_add_svo", "xn_server_submit", "xn_server_wait", "xn_server_stats",
+    "xn_server_add_svo", "xn_server_add_volume", "xn_server_submit", "xn_server_wait", "xn_server_stats",
     "xn_svo_load", "xn_svo_save", "xn_volume_save", "xn_volume_load", "xn_tiff_load", "xn_tiff_save",
     "xn_png_save",
 )
@@ -141,6 +141,7 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "xn_server_destroy": (i32, [vp]),
         "xn_server_add_grid": (i32, [vp, u32, vp, u32, u32, u32]),
         "xn_server_add_svo": (i32, [vp, u32, vp, u64, u64]),
+        "xn_server_add_volume": (i32, [vp, u32, vp]),
         "xn_server_submit": (i32, [vp, u32, i32, P(Camera), P(Params), vp, P(u64)]),
         "xn_server_wait": (i32, [vp, u64, ctypes.c_double, P(ctypes.c_double)]),
         "xn_server_stats": (i32, [vp, P(ServerStats)]),
@@ -392,7 +393,7 @@ class BatchGraph:
 class Server:
     """xn_server: continuous batching of render requests on one context."""
 
-    def __init__(self, ctx: Context, hbm_budget: int = 0, max_batch_jobs: int = 256, streams: int = 2):
+    def __init__(self, ctx: Context, hbm_budget: int = 0, max_batch_jobs: int = 256, streams: int = 3):
         self.ctx = ctx
         self.lib = ctx.lib
         cfg = ServerConfig(hbm_budget, max_batch_jobs, streams)
@@ -408,6 +409,10 @@ class Server:
     def add_svo(self, volume_id: int, nodes: np.ndarray, side: int) -> None:
         n = np.ascontiguousarray(nodes, dtype=np.uint32).reshape(-1, 10)
         _check(self.lib.xn_server_add_svo(self.handle, volume_id, n.ctypes.data, n.shape[0], int(side)))
+
+    def add_volume(self, volume_id: int, volume: "Volume") -> None:
+        """A volume already resident in the context; the caller keeps owning it."""
+        _check(self.lib.xn_server_add_volume(self.handle, volume_id, volume.handle))
 
     def submit(self, volume_id: int, traversal, camera: Camera, params: Params, out: np.ndarray | None = None) -> int:
         w, h = params.output_region.width, params.output_region.height

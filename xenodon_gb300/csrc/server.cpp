@@ -39,6 +39,7 @@ struct ServerVolume {
     std::vector<uint32_t> nodes;
     uint64_t side = 0;
     xn_volume* dev = nullptr;
+    bool external = false;    // the caller's resident volume: never evicted or released here
     uint64_t dev_bytes = 0;   // measured once resident
     uint64_t estimate = 0;    // before the first upload
     uint64_t last_use = 0;
@@ -59,13 +60,18 @@ struct Request {
     int status = 1;  // 1 pending, 0 done, < 0 error
 };
 
+// A stream slot: FREE, RUNNING (its batch is on the GPU) or COPYING (the GPU
+// is done; the copy thread moves the frames from the pinned staging buffer
+// into the callers' buffers, then frees the slot).
+enum class SlotState { FREE, RUNNING, COPYING };
+
 struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     void* staging = nullptr;
     uint64_t staging_bytes = 0;
     std::vector<Request*> reqs;
-    bool busy = false;
+    SlotState state = SlotState::FREE;
 };
 
 }  // namespace
@@ -76,9 +82,10 @@ struct xn_server {
     uint64_t budget = 0;
     uint64_t used = 0;  // resident volumes + outputs of admitted requests
     std::mutex mu;
-    std::condition_variable cv_work, cv_done;
-    bool stop = false;
-    std::thread worker;
+    std::condition_variable cv_work, cv_done, cv_copy;
+    bool stop = false, stop_copier = false;
+    std::thread worker, copier;
+    std::deque<size_t> copy_queue;  // slots whose frames wait for the copy thread
     std::map<uint32_t, ServerVolume> volumes;
     std::deque<Request*> pending;
     std::unordered_map<uint64_t, Request*> requests;
@@ -91,7 +98,13 @@ struct xn_server {
     bool any = false;
 
     void run();
+    void copy_run();
     bool retire_finished();
+    bool any_slot_in_use() const {
+        for (const auto& sl : slots)
+            if (sl.state != SlotState::FREE) return true;
+        return false;
+    }
     void launch_batch(Slot& slot);
     int make_resident(uint32_t id, ServerVolume& v, const std::vector<uint32_t>& protect);
 };
@@ -115,7 +128,7 @@ int xn_server::make_resident(uint32_t id, ServerVolume& v, const std::vector<uin
         bool found = false;
         for (auto& kv : volumes) {
             ServerVolume& o = kv.second;
-            if (!o.dev || o.refs > 0 || kv.first == id) continue;
+            if (!o.dev || o.external || o.refs > 0 || kv.first == id) continue;
             if (std::find(protect.begin(), protect.end(), kv.first) != protect.end()) continue;
             if (o.last_use < oldest) {
                 oldest = o.last_use;
@@ -142,34 +155,57 @@ int xn_server::make_resident(uint32_t id, ServerVolume& v, const std::vector<uin
     return XN_OK;
 }
 
+// Called with the server mutex held: slots whose batch finished on the GPU
+// go to the copy thread (their device outputs are freed here, stream-ordered);
+// a batch that failed on the device fails its requests.
 bool xn_server::retire_finished() {
     bool any_retired = false;
-    for (auto& slot : slots) {
-        if (!slot.busy) continue;
+    for (size_t k = 0; k < slots.size(); ++k) {
+        Slot& slot = slots[k];
+        if (slot.state != SlotState::RUNNING) continue;
         const cudaError_t q_state = cudaEventQuery(slot.done);
         if (q_state == cudaErrorNotReady) continue;
-        const auto now = Clock::now();
+        for (Request* q : slot.reqs) {
+            cudaFreeAsync(q->d_out, slot.stream);
+            q->d_out = nullptr;
+            used -= q->out_bytes;
+            volumes[q->volume_id].refs--;
+        }
         if (q_state != cudaSuccess) {
-            // the batch failed on the device: its requests fail, the slot is free again
             for (Request* q : slot.reqs) {
-                cudaFreeAsync(q->d_out, slot.stream);
-                q->d_out = nullptr;
-                used -= q->out_bytes;
-                volumes[q->volume_id].refs--;
                 q->status = XN_ERR_CUDA;
                 ++failed;
             }
             slot.reqs.clear();
-            slot.busy = false;
-            any_retired = true;
-            continue;
+            slot.state = SlotState::FREE;
+            cv_done.notify_all();
+        } else {
+            slot.state = SlotState::COPYING;
+            copy_queue.push_back(k);
+            cv_copy.notify_one();
         }
-        for (Request* q : slot.reqs) {
+        any_retired = true;
+    }
+    return any_retired;
+}
+
+// The copy thread: pinned staging -> callers' buffers, outside the mutex, so
+// the worker keeps launching while frames are copied out.
+void xn_server::copy_run() {
+    std::unique_lock<std::mutex> lk(mu);
+    for (;;) {
+        cv_copy.wait(lk, [&] { return stop_copier || !copy_queue.empty(); });
+        if (copy_queue.empty()) break;  // stopping and nothing left
+        const size_t k = copy_queue.front();
+        copy_queue.pop_front();
+        Slot& slot = slots[k];
+        std::vector<Request*> reqs = slot.reqs;
+        lk.unlock();
+        for (Request* q : reqs)
             std::memcpy(q->out, static_cast<uint8_t*>(slot.staging) + q->staging_off, q->out_bytes);
-            cudaFreeAsync(q->d_out, slot.stream);  // stream-ordered: no device-wide synchronisation
-            q->d_out = nullptr;
-            used -= q->out_bytes;
-            volumes[q->volume_id].refs--;
+        const auto now = Clock::now();
+        lk.lock();
+        for (Request* q : reqs) {
             q->t_done = now;
             q->status = 0;
             latencies_ms.push_back(ms_between(q->t_submit, now));
@@ -177,11 +213,10 @@ bool xn_server::retire_finished() {
             t_last = now;
         }
         slot.reqs.clear();
-        slot.busy = false;
-        any_retired = true;
+        slot.state = SlotState::FREE;
+        cv_done.notify_all();
+        cv_work.notify_all();
     }
-    if (any_retired) cv_done.notify_all();
-    return any_retired;
 }
 
 void xn_server::launch_batch(Slot& slot) {
@@ -262,7 +297,7 @@ void xn_server::launch_batch(Slot& slot) {
         return;
     }
     slot.reqs = std::move(batch);
-    slot.busy = true;
+    slot.state = SlotState::RUNNING;
     ++batches;
     batched_jobs += slot.reqs.size();
 }
@@ -272,21 +307,17 @@ void xn_server::run() {
     std::unique_lock<std::mutex> lk(mu);
     for (;;) {
         retire_finished();
-        if (stop) {
-            bool busy = false;
-            for (auto& s : slots) busy |= s.busy;
-            if (!busy) break;
-        }
+        if (stop && !any_slot_in_use()) break;
         if (!stop && !pending.empty()) {
             for (auto& slot : slots) {
                 if (pending.empty()) break;
-                if (!slot.busy) launch_batch(slot);
+                if (slot.state == SlotState::FREE) launch_batch(slot);
             }
         }
-        bool busy = false;
-        for (auto& s : slots) busy |= s.busy;
-        if (busy) {
-            // poll the in-flight batches; wake early for new requests
+        bool running = false;
+        for (auto& sl : slots) running |= sl.state == SlotState::RUNNING;
+        if (running || any_slot_in_use()) {
+            // poll the batches on the GPU; wake early for new requests or a freed slot
             cv_work.wait_for(lk, std::chrono::microseconds(100));
         } else if (pending.empty() && !stop) {
             cv_work.wait(lk, [&] { return stop || !pending.empty(); });
@@ -300,9 +331,9 @@ XN_API int xn_server_create(xn_ctx* ctx, const xn_server_config* cfg, xn_server*
     xn_server* s = new (std::nothrow) xn_server();
     if (!s) return fail(XN_ERR_NOMEM, "xn_server_create: out of host memory");
     s->ctx = ctx;
-    s->cfg = cfg ? *cfg : xn_server_config{0, 256, 2};
+    s->cfg = cfg ? *cfg : xn_server_config{0, 256, 3};
     if (s->cfg.max_batch_jobs <= 0) s->cfg.max_batch_jobs = 256;
-    if (s->cfg.streams <= 0) s->cfg.streams = 2;
+    if (s->cfg.streams <= 0) s->cfg.streams = 3;
     uint64_t used = 0, budget = 0;
     xn_ctx_memory(ctx, &used, &budget);
     s->budget = s->cfg.hbm_budget ? s->cfg.hbm_budget : budget;
@@ -320,6 +351,7 @@ XN_API int xn_server_create(xn_ctx* ctx, const xn_server_config* cfg, xn_server*
         }
     }
     s->worker = std::thread([s] { s->run(); });
+    s->copier = std::thread([s] { s->copy_run(); });
     *out = s;
     return XN_OK;
 }
@@ -333,9 +365,15 @@ XN_API int xn_server_destroy(xn_server* s) {
         s->pending.clear();
     }
     s->cv_work.notify_all();
-    if (s->worker.joinable()) s->worker.join();
+    if (s->worker.joinable()) s->worker.join();  // returns once every slot is free again
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop_copier = true;
+    }
+    s->cv_copy.notify_all();
+    if (s->copier.joinable()) s->copier.join();
     for (auto& kv : s->volumes)
-        if (kv.second.dev) xn_volume_release(kv.second.dev);
+        if (kv.second.dev && !kv.second.external) xn_volume_release(kv.second.dev);
     for (auto& sl : s->slots) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
         if (sl.done) cudaEventDestroy(sl.done);
@@ -374,6 +412,28 @@ XN_API int xn_server_add_svo(xn_server* s, uint32_t id, const uint32_t* nodes, u
     uint64_t n_inner = 0;
     for (uint64_t i = 0; i < n; ++i) n_inner += nodes[i * 10 + 9] < 0x80000000u ? 1 : 0;
     v.estimate = n_inner ? n_inner * 68 + (n - n_inner) * 32 : n * 40;
+    return XN_OK;
+}
+
+XN_API int xn_server_add_volume(xn_server* s, uint32_t id, xn_volume* volume) {
+    if (!s || !volume) return fail(XN_ERR_ARG, "xn_server_add_volume: NULL argument");
+    xn_volume_info info;
+    int r = xn_volume_info_get(volume, &info);
+    if (r) return r;
+    if (reinterpret_cast<xn::Volume*>(volume)->ctx != reinterpret_cast<xn::Ctx*>(s->ctx))
+        return fail(XN_ERR_ARG, "xn_server_add_volume: volume belongs to another context");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->volumes.count(id)) return fail(XN_ERR_ARG, "xn_server_add_volume: volume %u exists", id);
+    if (s->budget && s->used + info.device_bytes > s->budget)
+        return fail(XN_ERR_BUDGET, "xn_server_add_volume: %llu bytes exceed the HBM budget",
+                    (unsigned long long)info.device_bytes);
+    ServerVolume& v = s->volumes[id];
+    v.kind = info.kind;
+    v.dev = volume;
+    v.external = true;
+    v.dev_bytes = info.device_bytes;
+    v.estimate = info.device_bytes;
+    s->used += info.device_bytes;
     return XN_OK;
 }
 
