@@ -141,8 +141,10 @@ def test_resident_volumes_are_served_and_never_evicted(ctx, volumes_data):
             server.wait(t, timeout=60)
         st = server.stats()
         assert st["hbm_used"] <= budget
-        with pytest.raises(xg.XenodonError):
-            server.add_volume(8, lean)  # over the budget with the grid resident
+    with xg.Server(ctx, hbm_budget=size // 2) as small:
+        with pytest.raises(xg.XenodonError) as e:
+            small.add_volume(7, lean)
+        assert e.value.code == xg.XN_ERR_BUDGET
     # the owner's volume is still usable after the server is gone
     again, _, _ = ctx.render(lean, "esvo", cam, p)
     assert np.array_equal(again, alone)
