@@ -442,6 +442,47 @@ def measure_c3(ctx, xg, args):
     return result
 
 
+def measure_small_dda(ctx, xg, args):
+    """The reference's CPU-runnable case: plain DDA on the 128^3 blob grid
+    (16 Gaussian blobs, seed 0), one 512x512 frame from the camera line
+    `0 0 -0.8660254 0 1 0 0.5 0.5 2.5` (2x the extent on +z, 60 deg vertical
+    field of view); the GPU kernel beside the FP32 oracle on all host cores."""
+    import torch
+    import oracle
+    from xenodon_gb300 import volumes
+    g = volumes.blobs(128, seed=0)
+    vol = ctx.upload_grid(g)
+    cam_t = ((0.0, 0.0, -0.8660254), (0.0, 1.0, 0.0), (0.5, 0.5, 2.5))
+    cam = xg.make_camera(*cam_t)
+    p = xg.make_params(512, 512, EMISSION)
+    out = torch.empty((512, 512), dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        ctx.render_device(vol, "dda", cam, p, out.data_ptr(), None, None, stream.cuda_stream)
+    torch.cuda.synchronize()
+    reps = 200
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(reps):
+        ctx.render_device(vol, "dda", cam, p, out.data_ptr(), None, None, stream.cuda_stream)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    rgba, _, _ = ctx.render(vol, "dda", cam, p)
+    vol.release()
+    oracle.build()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ref = oracle.render("dda", grid=g, camera=oracle.make_camera(*cam_t), view=oracle.make_view(512, 512, EMISSION),
+                        threads=threads, want_loads=False)
+    cpu_s = time.perf_counter() - t0
+    diff = int(np.abs(rgba.astype(np.int32) - ref["rgba"].astype(np.int32)).max())
+    return {"workload": "dda, 128^3 blob grid (seed 0), 512x512, camera 2x the extent on +z, 60 deg VFOV",
+            "gpu_ms_per_frame": round(ms, 4), "gpu_mrays_s": round(512 * 512 / ms / 1e3, 1),
+            "cpu_oracle_mrays_s": round(512 * 512 / cpu_s / 1e6, 3), "cpu_threads": threads,
+            "max_rgba_diff_vs_oracle": diff}
+
+
 def measure_serving(ctx, xg, args, scene, residents):
     """Continuous batching of the serving mix vs one frame per launch.
 
@@ -671,7 +712,8 @@ def run_ours(args):
     if rank == 0 and not args.no_extras:
         # the 1024^3 and 2048^3 volumes stay resident for the serving mix
         args.residents = []
-        extras = [("batched", lambda: measure_batched(ctx, xg, args))]
+        extras = [("small_dda", lambda: measure_small_dda(ctx, xg, args)),
+                  ("batched", lambda: measure_batched(ctx, xg, args))]
         if args.c3_size:
             extras.append(("large", lambda: measure_c3(ctx, xg, args)))
         extras.append(("serving", lambda: measure_serving(ctx, xg, args, (grid, nodes, st["side"]), args.residents)))
