@@ -136,28 +136,19 @@ __device__ V3 trace_dda_tex(cudaTextureObject_t tex, uint32_t dx, uint32_t dy, u
     // the step arithmetic.  The fetch after the last step reads a texel the
     // sum never uses (in range or the zero border).
     V3 tx = tex_texel<NORM>(tex, px, py, pz);
-    // Every step raises the smallest side by t_delta >= 1 (|rd| <= 1), so a
-    // ray takes at most about dx+dy+dz+3 steps; the cap (twice that, plus 64)
-    // only guards against malformed input and is checked once per 4 steps.
-    const uint32_t cap4 = cap & ~3u;
     while (t < lim) {
-        if (iter >= cap4) { err |= 1u; break; }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            ++iter;
-            if (COUNT) ++loads;
-            // lessThanEqual(side, min(side.yzx, side.zxy)) is side.k == min of
-            // all three (the sides are finite and positive)
-            const float t0 = fminf(side.x, fminf(side.y, side.z));
-            if (side.x == t0) { side.x = side.x + t_delta.x; px += sgn.x; }
-            if (side.y == t0) { side.y = side.y + t_delta.y; py += sgn.y; }
-            if (side.z == t0) { side.z = side.z + t_delta.z; pz += sgn.z; }
-            const V3 next = tex_texel<NORM>(tex, px, py, pz);
-            total = total + tx * (t0 - t);
-            t = t0;
-            tx = next;
-            if (!(t < lim)) break;
-        }
+        if (++iter > cap) { err |= 1u; break; }
+        if (COUNT) ++loads;
+        // lessThanEqual(side, min(side.yzx, side.zxy)) is side.k == min of
+        // all three (the sides are finite and positive)
+        const float t0 = fminf(side.x, fminf(side.y, side.z));
+        if (side.x == t0) { side.x = side.x + t_delta.x; px += sgn.x; }
+        if (side.y == t0) { side.y = side.y + t_delta.y; py += sgn.y; }
+        if (side.z == t0) { side.z = side.z + t_delta.z; pz += sgn.z; }
+        const V3 next = tex_texel<NORM>(tex, px, py, pz);
+        total = total + tx * (t0 - t);
+        t = t0;
+        tx = next;
     }
     return total;
 }
@@ -873,7 +864,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) dda_kernel(Frame f, GridVol g, 
 }
 
 template <bool COUNT, bool NORM>
-__global__ void __launch_bounds__(BLOCK_THREADS, 16) dda_tex_kernel(Frame f, cudaTextureObject_t tex, uint32_t dx,
+__global__ void __launch_bounds__(BLOCK_THREADS) dda_tex_kernel(Frame f, cudaTextureObject_t tex, uint32_t dx,
                                                                uint32_t dy, uint32_t dz, Outputs o) {
     uint32_t ix, iy;
     if (!pixel_of_thread(f, ix, iy)) return;
