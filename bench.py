@@ -132,6 +132,18 @@ def setup_dist(n_gpus: int):
     return world, rank, local, dist
 
 
+def aggregate_replicas(total_ms: float, rays_local: int, world: int, dist, device: str = "cpu"):
+    """Replicas (one per GPU, no exchange): the timed region of the job is the
+    slowest rank's; every rank renders rays_local rays.  Returns (max ms,
+    whole-job Mrays/s)."""
+    if dist:
+        import torch
+        t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return total_ms, rays_local * world / (total_ms * 1e3)
+
+
 def make_scene(device: int):
     import torch
     from xenodon_gb300 import cameras, volumes
@@ -637,13 +649,9 @@ def run_ours(args):
                for ti, t in enumerate(TRAVERSALS)}
     if ctx.ray_errors():
         print("warning: rays hit an iteration cap", file=sys.stderr)
-    if dist:
-        tt = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
     rays_per_frame = WIDTH * HEIGHT
-    total_rays = rays_per_frame * len(TRAVERSALS) * len(frames) * world
-    value = total_rays / (total_ms * 1e3)
+    total_ms, value = aggregate_replicas(total_ms, rays_per_frame * len(TRAVERSALS) * len(frames), world, dist,
+                                         "cuda")
     per = {t: rays_per_frame * len(frames) / (kern_ms[t] * 1e3) for t in TRAVERSALS}
 
     # algorithmic bytes: 4 B per reference word read + 4 B per pixel store
