@@ -155,6 +155,20 @@ __device__ V3 trace_dda_tex(cudaTextureObject_t tex, uint32_t dx, uint32_t dy, u
 
 // --------------------------------------------------------------- octree ---
 
+// UNORM8 -> float of leaf colours from a 256-entry table in shared memory,
+// filled with unorm8 itself (the same bits) by every octree kernel before its
+// first leaf: two instructions per channel instead of five.
+__shared__ float s_unorm_lut[256];
+
+__device__ __forceinline__ void fill_unorm_lut() {
+    for (uint32_t i = threadIdx.x; i < 256u; i += blockDim.x) s_unorm_lut[i] = unorm8(i);
+    __syncthreads();
+}
+
+__device__ __forceinline__ V3 leaf_rgb(uint32_t col) {
+    return V3{s_unorm_lut[col & 0xFFu], s_unorm_lut[(col >> 8) & 0xFFu], s_unorm_lut[(col >> 16) & 0xFFu]};
+}
+
 // Reference node layout on the device: 10 u32 words per node
 // (resources/octree.glsl:6-10).  Node handles are node indices.
 struct RefNodes {
@@ -356,7 +370,7 @@ __device__ V3 trace_naive(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t&
         u_min = fmaxf(u_min, 0.0f);
         float step = fmaxf(u_max - u_min, MIN_STEP);
         t += step;
-        V3 color = unpack_rgb(a.color(node));
+        V3 color = leaf_rgb(a.color(node));
         if (COUNT) ++loads;
         total = total + color * step;
     }
@@ -390,7 +404,7 @@ __device__ V3 trace_df(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& er
         if (t_min < t_max && t_max > 0.0f) {
             if (COUNT) ++loads;
             if (a.is_leaf(child)) {
-                V3 color = unpack_rgb(a.color(child));
+                V3 color = leaf_rgb(a.color(child));
                 if (COUNT) ++loads;
                 total = total + color * (t_max - fmaxf(t_min, 0.0f));
             } else {
@@ -570,7 +584,7 @@ __device__ V3 trace_df_masked(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint3
         float t0, t1;
         child_span(slabs, k, t0, t1);
         if (a.is_leaf(child)) {
-            const V3 color = unpack_rgb(a.color(child));
+            const V3 color = leaf_rgb(a.color(child));
             if (COUNT) ++loads;
             total = total + color * (t1 - fmaxf(t0, 0.0f));
             continue;
@@ -650,7 +664,7 @@ __device__ V3 trace_esvo(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& 
                 uint32_t child = a.child(parent, idx ^ octant_mask);
                 if (COUNT) loads += 2;
                 if (a.is_leaf(child)) {
-                    V3 color = unpack_rgb(a.color(child));
+                    V3 color = leaf_rgb(a.color(child));
                     if (COUNT) ++loads;
                     total = total + color * (tv_max - t_min);
                 } else {
@@ -774,7 +788,7 @@ __device__ V3 trace_rope(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& 
     float u_min = max_elem(vmin(node_min, node_max));
     float u_max = min_elem(far);
     float step = u_max - fmaxf(u_min, 0.0f);
-    V3 color = unpack_rgb(a.color(node));
+    V3 color = leaf_rgb(a.color(node));
     V3 total = color * step;
     V3 mask;
     uint32_t n = neighbor_index(nbx, nby, nbz, far, mask);
@@ -792,7 +806,7 @@ __device__ V3 trace_rope(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& 
         u_min = max_elem(vmin(node_min, node_max));
         u_max = min_elem(far);
         step = u_max - fmaxf(u_min, 0.0f);
-        color = unpack_rgb(a.color(node));
+        color = leaf_rgb(a.color(node));
         total = total + color * step;
         n = neighbor_index(nbx, nby, nbz, far, mask);
         node = a.child(node, n);
@@ -880,6 +894,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) dda_tex_kernel(Frame f, cudaTex
 
 template <int TRAV, bool COUNT, class Acc>
 __global__ void __launch_bounds__(BLOCK_THREADS) svo_kernel(Frame f, Acc a, Outputs o) {
+    fill_unorm_lut();
     uint32_t ix, iy;
     if (!pixel_of_thread(f, ix, iy)) return;
     V3 rd = primary_ray(f, ix, iy);
@@ -1003,7 +1018,7 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
             if (mine) {
                 float t0, t1;
                 child_span(slabs, k, t0, t1);
-                const V3 color = unpack_rgb(a.color(child));
+                const V3 color = leaf_rgb(a.color(child));
                 if (COUNT) ++loads;
                 total = total + color * (t1 - fmaxf(t0, 0.0f));
             }
@@ -1042,6 +1057,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) df_packet_kernel(Frame f, Acc a
     __shared__ uint32_t s_node[(BLOCK_THREADS / 32) * STACK_DEPTH];
     __shared__ uint32_t s_state[(BLOCK_THREADS / 32) * STACK_DEPTH];
     __shared__ uint8_t s_mask[(BLOCK_THREADS / 32) * STACK_DEPTH * 32];
+    fill_unorm_lut();
     const uint32_t warp = threadIdx.x >> 5;
     uint32_t ix, iy;
     const bool active = pixel_of_thread(f, ix, iy);
@@ -1064,6 +1080,7 @@ template <int TRAV, bool COUNT, class Acc>
 __global__ void __launch_bounds__(SHARED_BLOCK) shared_stack_kernel(Frame f, Acc a, Outputs o) {
     __shared__ uint32_t s_a[STACK_DEPTH * SHARED_BLOCK];
     __shared__ uint32_t s_b[STACK_DEPTH * SHARED_BLOCK];
+    fill_unorm_lut();
     uint32_t ix, iy;
     if (!pixel_of_thread_bt<SHARED_BLOCK>(f, ix, iy)) return;
     SharedStacks stk{s_a + threadIdx.x, s_b + threadIdx.x, SHARED_BLOCK};
@@ -1385,6 +1402,7 @@ constexpr int batch_min_blocks(int spec) {
 template <int TW, int SPEC>
 __global__ void __launch_bounds__(1024, batch_min_blocks(SPEC)) batch_kernel(const BatchHeader* hdr, const BatchJob* jobs,
                                                      unsigned long long* queue, uint32_t chunk, uint32_t* err_word) {
+    fill_unorm_lut();
     constexpr int TH = 32 / TW;
     // esvo and svo-df stacks: two columns per thread in dynamic shared memory
     // (2 * STACK_DEPTH words a thread, given at launch for the forms that use them)
@@ -1426,6 +1444,7 @@ __global__ void __launch_bounds__(1024, batch_min_blocks(SPEC)) batch_kernel(con
 template <int TW, int SPEC>
 __global__ void __launch_bounds__(1024, batch_min_blocks(SPEC)) batch_grid_kernel(const BatchHeader* hdr, const BatchJob* jobs,
                                                           uint32_t* err_word) {
+    fill_unorm_lut();
     constexpr int TH = 32 / TW;
     extern __shared__ uint32_t batch_stacks[];
     SharedStacks stk{batch_stacks + threadIdx.x, batch_stacks + STACK_DEPTH * blockDim.x + threadIdx.x, blockDim.x};
