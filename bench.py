@@ -650,6 +650,7 @@ def run_ours(args):
     if ctx.ray_errors():
         print("warning: rays hit an iteration cap", file=sys.stderr)
     rays_per_frame = WIDTH * HEIGHT
+    total_rays = rays_per_frame * len(TRAVERSALS) * len(frames) * world
     total_ms, value = aggregate_replicas(total_ms, rays_per_frame * len(TRAVERSALS) * len(frames), world, dist,
                                          "cuda")
     per = {t: rays_per_frame * len(frames) / (kern_ms[t] * 1e3) for t in TRAVERSALS}
