@@ -332,3 +332,18 @@ def test_df_walked_by_the_warp_equals_one_ray_per_thread(ctx, blob_volumes, monk
     _, em_0, loads_0 = _gpu_counts(ctx, vol, "svo-df", xg.make_camera(*CAMS[cam]), p)
     assert np.array_equal(packet, plain)
     assert np.array_equal(em_p, em_0) and np.array_equal(loads_p, loads_0)
+
+
+@pytest.mark.parametrize("cam", ["front", "inside", "grazing"])
+def test_dda_raw_texel_reads_equal_normalized(ctx, blob_volumes, monkeypatch, cam):
+    # XN_TEX_READ=raw: the texture returns the bytes and the kernel converts
+    # them through its shared table; same bits as the texture unit's UNORM read
+    import xenodon_gb300 as xg
+    g, _, _ = blob_volumes
+    p, v = _params_pair(xg, 77, 53)
+    norm_vol = ctx.upload_grid(g)
+    a, _ = check_parity(ctx, "dda", CAMS[cam], p, v, grid=g, vol=norm_vol, label=f"dda-norm/{cam}")
+    monkeypatch.setenv("XN_TEX_READ", "raw")
+    raw_vol = ctx.upload_grid(g)
+    b, _ = check_parity(ctx, "dda", CAMS[cam], p, v, grid=g, vol=raw_vol, label=f"dda-raw/{cam}")
+    assert np.array_equal(a, b)

@@ -279,7 +279,10 @@ int upload_grid(xn_ctx* h, const uint8_t* rgba, bool from_device, uint32_t dx, u
     }
     cudaError_t e = cudaSuccess;
     if (use_tex) {
-        const bool norm = texture_unorm_exact(c) == 1;
+        // the texture unit converts to float when it gives byte/255 exactly,
+        // unless XN_TEX_READ=raw (4-byte texels, converted in the kernel)
+        const char* rd = std::getenv("XN_TEX_READ");
+        const bool norm = !(rd && std::strcmp(rd, "raw") == 0) && texture_unorm_exact(c) == 1;
         if (c->budget && c->used.load() + bytes > c->budget) {
             delete v;
             return fail(XN_ERR_BUDGET, "xn_volume_upload_grid: %llu bytes exceed the HBM budget",

@@ -96,14 +96,29 @@ __device__ V3 trace_dda(const GridVol& g, V3 ro, V3 rd, uint32_t& loads, uint32_
 // the address arithmetic to the texture unit.  NORM: the unit returns
 // byte/255 (used when that conversion is exact, see xn_volume_upload_grid);
 // otherwise the raw bytes are converted with unorm8.
+// UNORM8 -> float of leaf colours from a 256-entry table in shared memory,
+// filled with unorm8 itself (the same bits) by every octree kernel before its
+// first leaf: two instructions per channel instead of five.
+__shared__ float s_unorm_lut[256];
+
+__device__ __forceinline__ void fill_unorm_lut() {
+    for (uint32_t i = threadIdx.x; i < 256u; i += blockDim.x) s_unorm_lut[i] = unorm8(i);
+    __syncthreads();
+}
+
+__device__ __forceinline__ V3 leaf_rgb(uint32_t col) {
+    return V3{s_unorm_lut[col & 0xFFu], s_unorm_lut[(col >> 8) & 0xFFu], s_unorm_lut[(col >> 16) & 0xFFu]};
+}
+
 template <bool NORM>
 __device__ __forceinline__ V3 tex_texel(cudaTextureObject_t t, float x, float y, float z) {
     if (NORM) {
         float4 v = tex3D<float4>(t, x, y, z);
         return V3{v.x, v.y, v.z};
     }
+    // raw bytes, converted through the shared table (the kernel fills it)
     uchar4 v = tex3D<uchar4>(t, x, y, z);
-    return V3{unorm8(v.x), unorm8(v.y), unorm8(v.z)};
+    return V3{s_unorm_lut[v.x], s_unorm_lut[v.y], s_unorm_lut[v.z]};
 }
 
 // resources/dda.comp:13-53 over the texture form; coordinates are kept as
@@ -154,20 +169,6 @@ __device__ V3 trace_dda_tex(cudaTextureObject_t tex, uint32_t dx, uint32_t dy, u
 }
 
 // --------------------------------------------------------------- octree ---
-
-// UNORM8 -> float of leaf colours from a 256-entry table in shared memory,
-// filled with unorm8 itself (the same bits) by every octree kernel before its
-// first leaf: two instructions per channel instead of five.
-__shared__ float s_unorm_lut[256];
-
-__device__ __forceinline__ void fill_unorm_lut() {
-    for (uint32_t i = threadIdx.x; i < 256u; i += blockDim.x) s_unorm_lut[i] = unorm8(i);
-    __syncthreads();
-}
-
-__device__ __forceinline__ V3 leaf_rgb(uint32_t col) {
-    return V3{s_unorm_lut[col & 0xFFu], s_unorm_lut[(col >> 8) & 0xFFu], s_unorm_lut[(col >> 16) & 0xFFu]};
-}
 
 // Reference node layout on the device: 10 u32 words per node
 // (resources/octree.glsl:6-10).  Node handles are node indices.
@@ -880,6 +881,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) dda_kernel(Frame f, GridVol g, 
 template <bool COUNT, bool NORM>
 __global__ void __launch_bounds__(BLOCK_THREADS) dda_tex_kernel(Frame f, cudaTextureObject_t tex, uint32_t dx,
                                                                uint32_t dy, uint32_t dz, Outputs o) {
+    if (!NORM) fill_unorm_lut();
     uint32_t ix, iy;
     if (!pixel_of_thread(f, ix, iy)) return;
     uint32_t m = max(dx, max(dy, dz));
