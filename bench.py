@@ -597,6 +597,20 @@ def measure_serving(ctx, xg, args, scene, residents):
     return result
 
 
+def run_dda_4k_only(args):
+    import torch
+    import xenodon_gb300 as xg
+    from xenodon_gb300 import build as native, volumes
+    native.build()
+    ctx = xg.Context(0)
+    g = volumes.gas_field(args.dda_4k, seed=2, device="cuda", as_tensor=True)
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    print(json.dumps(measure_dda_4k(ctx, xg, g, args.dda_4k)))
+    ctx.close()
+    return 0
+
+
 def run_ours(args):
     import torch
     import xenodon_gb300 as xg
@@ -765,12 +779,16 @@ def main(argv=None):
     ap.add_argument("--batched-size", type=int, default=1024)
     ap.add_argument("--batched-cameras", type=int, default=64)
     ap.add_argument("--c3-size", type=int, default=2048, help="grid size of the large workload (0: skip it)")
+    ap.add_argument("--dda-4k", type=int, default=0, metavar="N",
+                    help="only the 3840x2160 DDA measurement on an N^3 gas field (for profiling); prints its line")
     ap.add_argument("--c3-frames", type=int, default=16)
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 200.0, 1000.0, 2000.0, 0.0])
     args = ap.parse_args(argv)
     if args.impl == "reference":
         return run_reference(args)
+    if args.dda_4k:
+        return run_dda_4k_only(args)
     return run_ours(args)
 
 
