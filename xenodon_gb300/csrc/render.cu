@@ -270,8 +270,9 @@ constexpr int FIX_BITS = 30;
 constexpr int FIX_DEPTH = 24;
 
 __device__ __forceinline__ uint32_t fix_coord(float p) {
-    const float q = floorf(fminf(fmaxf(p, -1.0f), 1.5f) * 1073741824.0f);  // * 2^30, exact
-    const int v = (int)q;
+    // floor(p * 2^30) (the scaling is exact); the conversion saturates and
+    // the clamp then gives the open bounds of the border cells
+    const int v = __float2int_rd(p * 1073741824.0f);
     return (uint32_t)min(max(v, 0), (1 << FIX_BITS) - 1);
 }
 
