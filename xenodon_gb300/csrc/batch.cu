@@ -73,7 +73,9 @@ uint32_t resident_blocks(Ctx* c, const xn_batch_config& cfg) {
     return (uint32_t)per_sm * (uint32_t)c->sm_count();
 }
 
-xn_batch_config default_config() { return xn_batch_config{8, 128, 0, 1}; }
+// 4x8 warp tiles, blocks of 256, no queue: the shape the autotuner picked most
+// often (CT frames and the 1024^3 and 2048^3 gas fields, every traversal).
+xn_batch_config default_config() { return xn_batch_config{4, 256, 0, 0}; }
 
 // Pinned staging for the job tables of xn_render_batch (one per context; a
 // new table is written only after the previous one was copied out).

@@ -32,6 +32,10 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// Frames of at least this many pixels fill the GPU in one launch (a GB300 holds
+// 152 x 2048 resident threads).
+constexpr uint64_t LARGE_FRAME = 1ull << 19;
+
 struct ServerVolume {
     int kind = 0;
     std::vector<uint8_t> grid;
@@ -277,7 +281,19 @@ void xn_server::launch_batch(Slot& slot) {
         slot.staging_bytes = 0;
         if (cudaHostAlloc(&slot.staging, staging, cudaHostAllocDefault) == cudaSuccess) slot.staging_bytes = staging;
     }
-    int r = slot.staging ? xn_render_batch(ctx, jobs.data(), (int)jobs.size(), nullptr, slot.stream) : XN_ERR_NOMEM;
+    // frames big enough to fill the GPU alone go to the single-frame kernels
+    // (they gain nothing from the batch kernel); the rest share one batch
+    std::vector<xn_job> small;
+    int r = slot.staging ? XN_OK : XN_ERR_NOMEM;
+    for (size_t i = 0; !r && i < jobs.size(); ++i) {
+        const xn_rect& o = jobs[i].params.output_region;
+        if ((uint64_t)o.width * o.height >= LARGE_FRAME)
+            r = xn_render_device(ctx, jobs[i].volume, jobs[i].traversal, &jobs[i].camera, &jobs[i].params,
+                                 jobs[i].d_rgba, nullptr, nullptr, slot.stream);
+        else
+            small.push_back(jobs[i]);
+    }
+    if (!r && !small.empty()) r = xn_render_batch(ctx, small.data(), (int)small.size(), nullptr, slot.stream);
     for (size_t i = 0; !r && i < batch.size(); ++i)
         if (cudaMemcpyAsync(static_cast<uint8_t*>(slot.staging) + batch[i]->staging_off, batch[i]->d_out,
                             batch[i]->out_bytes, cudaMemcpyDeviceToHost, slot.stream) != cudaSuccess)
