@@ -183,9 +183,11 @@ typedef struct {
 } xn_batch_config;
 
 /* Renders n_jobs frames of any mix of volumes, traversals and resolutions in
- * one persistent launch on `stream` (returns without synchronising): resident
- * warps pull tiles from one global queue.  cfg NULL = the configuration the
- * autotuner chose for this mix of traversals, else a default. */
+ * one launch on `stream` (returns without synchronising).  With a queue
+ * (chunk >= 1) resident warps pull tiles from one global counter; with chunk
+ * 0, a grid holds one warp per tile.  cfg NULL means the configuration the
+ * autotuner chose for this mix of traversals, else 4x8 tiles in blocks of 256
+ * with no queue. */
 XN_API int xn_render_batch(xn_ctx* ctx, const xn_job* jobs, int n_jobs, const xn_batch_config* cfg, void* stream);
 
 /* Times xn_render_batch over a sweep of launch shapes on the given jobs and
@@ -204,16 +206,19 @@ XN_API int xn_batch_graph_destroy(xn_batch_graph* g);
 
 /* ----------------------------------------------------------- serving --- */
 
-/* A render server (no counterpart in the reference): a worker thread keeps
+/* A render server (no counterpart in the reference).  A worker thread keeps
  * registered volumes resident with least-recently-used eviction under an HBM
- * budget, admits requests in arrival order as memory allows, renders each
- * admitted set as one persistent batch on one of `streams` CUDA streams, and
- * admits newly arrived requests while earlier batches are still running. */
+ * budget and admits requests in arrival order as memory allows.  Each
+ * admitted set goes to one of `streams` CUDA streams: frames of 2^19 pixels or
+ * more (each fills the GPU alone) through the single-frame kernels, the
+ * smaller ones as one batch.  Newly arrived requests are admitted while
+ * earlier batches still run.  A copy thread moves finished frames into the
+ * callers' buffers. */
 typedef struct xn_server xn_server;
 typedef struct {
     uint64_t hbm_budget; /* bytes for resident volumes and in-flight frames; 0 = the context's budget */
     int max_batch_jobs;  /* requests per persistent launch (default 256) */
-    int streams;         /* batches in flight at once (default 2) */
+    int streams;         /* batches in flight at once (default 3) */
 } xn_server_config;
 typedef struct {
     uint64_t completed, failed, batches, uploads, evictions, rays, hbm_used;
