@@ -155,3 +155,30 @@ def test_single_traversal_batches_use_the_inlined_form(ctx, scene, monkeypatch, 
             torch.cuda.synchronize()
             for b, r in zip(bufs, ref):
                 assert np.array_equal(b.cpu().numpy(), r), (trav, generic)
+
+
+@pytest.mark.parametrize("generic", ["0", "1"])
+def test_mixed_batches_split_by_form_or_generic_agree(ctx, scene, monkeypatch, generic):
+    # a mixed batch runs one specialised launch per form (default) or one
+    # generic launch (XN_BATCH_GENERIC=1); graphs capture the same choice
+    import torch
+    xg, _ = scene
+    monkeypatch.setenv("XN_BATCH_GENERIC", generic)
+    specs = _specs(scene)
+    ref = _reference_frames(ctx, specs)
+    stream = torch.cuda.current_stream().cuda_stream
+    bufs = _batch_buffers(specs)
+    jobs = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs, bufs))
+    ctx.render_batch(jobs, len(specs), xg.BatchConfig(4, 256, 0, 0), stream)
+    torch.cuda.synchronize()
+    for b, r in zip(bufs, ref):
+        assert np.array_equal(b.cpu().numpy(), r)
+    g = ctx.batch_graph(len(specs), xg.BatchConfig(8, 128, 0, 1), stream)
+    for _ in range(2):
+        bufs = _batch_buffers(specs)
+        jobs = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs, bufs))
+        g.launch(jobs, len(specs))
+        torch.cuda.synchronize()
+        for b, r in zip(bufs, ref):
+            assert np.array_equal(b.cpu().numpy(), r)
+    g.close()

@@ -99,7 +99,53 @@ int ensure_batch_staging(Ctx* c, uint64_t bytes) {
 // Every launch gets a device job table and work counter of its own, allocated
 // and freed in the order of its stream: launches on other streams (the render
 // server runs several) never see them, and no launch waits for another.
+// The kernel form (XN_BATCH_*) each job needs.
+int forms_of(Ctx* c, const xn_job* jobs, int n, std::vector<int>& forms) {
+    forms.resize(n);
+    for (int i = 0; i < n; ++i) {
+        if (!jobs[i].volume || !jobs[i].d_rgba) return fail(XN_ERR_ARG, "batch: job %d has no volume or output", i);
+        const Volume* v = reinterpret_cast<const Volume*>(jobs[i].volume);
+        if (v->ctx != c) return fail(XN_ERR_ARG, "batch: job %d uses a volume of another context", i);
+        RenderLaunch L;
+        int r = make_launch(v, jobs[i].traversal, &jobs[i].camera, &jobs[i].params, L);
+        if (r) return r;
+        forms[i] = batch_spec(make_batch_job(L));
+    }
+    return XN_OK;
+}
+
+bool generic_forced() {
+    const char* generic = std::getenv("XN_BATCH_GENERIC");
+    return generic && generic[0] == '1';
+}
+
+int render_batch_one(Ctx* c, const xn_job* jobs, int n, const xn_batch_config& cfg, cudaStream_t s);
+
+// A batch whose jobs need different kernel forms runs as one launch per form
+// (each specialised, each over its own jobs, in the stream's order); with
+// XN_BATCH_GENERIC=1 the generic form takes the whole batch in one launch.
 int render_batch_locked(Ctx* c, const xn_job* jobs, int n, const xn_batch_config& cfg, cudaStream_t s) {
+    if (!generic_forced()) {
+        std::vector<int> forms;
+        int r = forms_of(c, jobs, n, forms);
+        if (r) return r;
+        bool mixed = false;
+        for (int i = 1; i < n; ++i) mixed |= forms[i] != forms[0];
+        if (mixed) {
+            std::vector<xn_job> part;
+            for (int f = 0; f < XN_BATCH_FORMS && !r; ++f) {
+                part.clear();
+                for (int i = 0; i < n; ++i)
+                    if (forms[i] == f) part.push_back(jobs[i]);
+                if (!part.empty()) r = render_batch_one(c, part.data(), (int)part.size(), cfg, s);
+            }
+            return r;
+        }
+    }
+    return render_batch_one(c, jobs, n, cfg, s);
+}
+
+int render_batch_one(Ctx* c, const xn_job* jobs, int n, const xn_batch_config& cfg, cudaStream_t s) {
     const uint64_t cap = sizeof(BatchHeader) + (uint64_t)n * sizeof(BatchJob);
     int r = ensure_batch_staging(c, cap);
     if (r) return r;
@@ -109,8 +155,7 @@ int render_batch_locked(Ctx* c, const xn_job* jobs, int n, const xn_batch_config
     int spec = XN_BATCH_ANY;
     if ((r = fill_table(c, jobs, n, cfg.tile_width, c->batch_host, c->batch_host_bytes, &bytes, &spec))) return r;
     // XN_BATCH_GENERIC=1 keeps the generic form (same results)
-    const char* generic = std::getenv("XN_BATCH_GENERIC");
-    if (generic && generic[0] == '1') spec = XN_BATCH_ANY;
+    if (generic_forced()) spec = XN_BATCH_ANY;
     const uint64_t queue_off = (bytes + 255) & ~255ull;
     void* d = nullptr;
     e = cudaMallocAsync(&d, queue_off + 256, s);
@@ -217,13 +262,17 @@ XN_API int xn_autotune_batch(xn_ctx* h, const xn_job* jobs, int n, void* stream,
 
 // ------------------------------------------------------------------ graphs
 
+// A batch graph captures one launch per kernel form, each over its own
+// segment of the job table (a form without jobs exits at once), or with
+// XN_BATCH_GENERIC=1 one generic launch over the whole table.
 struct xn_batch_graph {
     Ctx* ctx;
     cudaStream_t stream;
     xn_batch_config cfg;
-    int spec = XN_BATCH_ANY;  // captured once for any jobs: the generic form
+    bool split = true;
     int capacity;
-    uint64_t table_bytes;
+    uint64_t seg_bytes;    // one form's segment: header + capacity jobs
+    uint64_t table_bytes;  // all segments
     struct Slot {
         void* host = nullptr;
         void* dev = nullptr;
@@ -247,7 +296,7 @@ void destroy_graph(xn_batch_graph* g) {
         if (s.exec) cudaGraphExecDestroy(s.exec);
         if (s.host) cudaFreeHost(s.host);
         c->device_free(s.dev, g->table_bytes);
-        c->device_free(s.queue, 64);
+        c->device_free(s.queue, 64 * XN_BATCH_FORMS);
     }
     delete g;
 }
@@ -269,7 +318,9 @@ XN_API int xn_batch_graph_create(xn_ctx* h, int capacity, const xn_batch_config*
     g->cfg = cfg ? *cfg : default_config();
     if (g->cfg.chunk == 0) g->cfg.chunk = 1;  // the tile count changes per replay: graphs use the queue form
     g->capacity = capacity;
-    g->table_bytes = sizeof(BatchHeader) + (uint64_t)capacity * sizeof(BatchJob);
+    g->split = !generic_forced();
+    g->seg_bytes = (sizeof(BatchHeader) + (uint64_t)capacity * sizeof(BatchJob) + 255) & ~255ull;
+    g->table_bytes = g->seg_bytes * (g->split ? XN_BATCH_FORMS : 1);
     if ((r = check_config(g->cfg))) {
         delete g;
         return r;
@@ -280,16 +331,20 @@ XN_API int xn_batch_graph_create(xn_ctx* h, int capacity, const xn_batch_config*
     for (auto& sl : g->slot) {
         if (e != cudaSuccess || r) break;
         if ((e = cudaHostAlloc(&sl.host, g->table_bytes, cudaHostAllocDefault)) != cudaSuccess) break;
-        std::memset(sl.host, 0, sizeof(BatchHeader));
+        std::memset(sl.host, 0, g->table_bytes);
         if ((r = c->device_alloc(&sl.dev, g->table_bytes, "xn_batch_graph_create: job table"))) break;
-        if ((r = c->device_alloc(reinterpret_cast<void**>(&sl.queue), 64, "xn_batch_graph_create: queue"))) break;
+        if ((r = c->device_alloc(reinterpret_cast<void**>(&sl.queue), 64 * XN_BATCH_FORMS,
+                                 "xn_batch_graph_create: queue")))
+            break;
         if ((e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming)) != cudaSuccess) break;
-        // capture: table upload, queue reset, persistent kernel
+        // capture: table upload, queue resets, one persistent launch per form
         if ((e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
         cudaMemcpyAsync(sl.dev, sl.host, g->table_bytes, cudaMemcpyHostToDevice, cap);
-        cudaMemsetAsync(sl.queue, 0, 8, cap);
-        launch_batch(sl.dev, sl.queue, c->d_err, g->cfg.tile_width, g->cfg.block_threads, blocks, g->cfg.chunk,
-                     g->spec, cap);
+        cudaMemsetAsync(sl.queue, 0, 64 * XN_BATCH_FORMS, cap);
+        const int n_launch = g->split ? XN_BATCH_FORMS : 1;
+        for (int f = 0; f < n_launch; ++f)
+            launch_batch(static_cast<char*>(sl.dev) + f * g->seg_bytes, sl.queue + f * 8, c->d_err, g->cfg.tile_width,
+                         g->cfg.block_threads, blocks, g->cfg.chunk, g->split ? f : XN_BATCH_ANY, cap);
         cudaGraph_t graph = nullptr;
         e = cudaStreamEndCapture(cap, &graph);
         if (e == cudaSuccess) e = cudaGraphInstantiate(&sl.exec, graph, 0);
@@ -314,7 +369,21 @@ XN_API int xn_batch_graph_launch(xn_batch_graph* g, const xn_job* jobs, int n) {
     auto& sl = g->slot[g->next];
     if (sl.pending) cudaEventSynchronize(sl.done);  // this slot's previous batch has finished
     uint64_t bytes = 0;
-    if ((r = fill_table(c, jobs, n, g->cfg.tile_width, sl.host, g->table_bytes, &bytes))) return r;
+    if (g->split) {
+        std::vector<int> forms;
+        if ((r = forms_of(c, jobs, n, forms))) return r;
+        std::vector<xn_job> part;
+        for (int f = 0; f < XN_BATCH_FORMS; ++f) {
+            part.clear();
+            for (int i = 0; i < n; ++i)
+                if (forms[i] == f) part.push_back(jobs[i]);
+            if ((r = fill_table(c, part.data(), (int)part.size(), g->cfg.tile_width,
+                                static_cast<char*>(sl.host) + f * g->seg_bytes, g->seg_bytes, &bytes)))
+                return r;
+        }
+    } else if ((r = fill_table(c, jobs, n, g->cfg.tile_width, sl.host, g->table_bytes, &bytes))) {
+        return r;
+    }
     cudaError_t e = cudaGraphLaunch(sl.exec, g->stream);
     if (e == cudaSuccess) e = cudaEventRecord(sl.done, g->stream);
     if (e != cudaSuccess) return cuda_fail(e, "xn_batch_graph_launch");

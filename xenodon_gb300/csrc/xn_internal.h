@@ -93,7 +93,7 @@ BatchJob make_batch_job(const RenderLaunch& L);
 // Batch kernel forms: one traversal (and layout) inlined when every job of
 // the batch shares it, else the generic per-pixel dispatch.
 enum { XN_BATCH_ANY = 0, XN_BATCH_DDA_TEX_NORM, XN_BATCH_DDA_TEX_RAW, XN_BATCH_ESVO, XN_BATCH_NAIVE, XN_BATCH_DF,
-       XN_BATCH_ROPE };
+       XN_BATCH_ROPE, XN_BATCH_FORMS };
 // The form a job needs (XN_BATCH_*).
 int batch_spec(const BatchJob& j);
 // Launches the persistent kernel over a job table already in device memory
