@@ -499,43 +499,6 @@ __device__ __forceinline__ void child_span(const ChildSlabs& c, uint32_t k, floa
     t1 = fminf(bx ? c.xh1 : c.xh0, fminf(by ? c.yh1 : c.yh0, bz ? c.zh1 : c.zh0));
 }
 
-// The slabs of child k from its parent's.  Per axis the parent's plane
-// distances at O, O+s and O+2s are ordered by the sign of rrd (monotone
-// rounding), so the parent's min/max pairs give them back exactly.  The
-// child's outer planes are two of them, computed by the same expressions on
-// the same (dyadic, exact) positions; only the child's midplane
-// (O_c + s_c) * rrd - bias is new.  Equal to child_slabs(O_c, s_c, ...) bit
-// for bit.
-__device__ __forceinline__ float2 child_axis(float l0, float l1, float h0, float h1, bool pos, bool bit, float mid,
-                                             float& lo1, float& hi1) {
-    const float p0 = pos ? l0 : h0;  // plane at O
-    const float p1 = pos ? h0 : l0;  // plane at O + s
-    const float p2 = pos ? h1 : l1;  // plane at O + 2s
-    const float c0 = bit ? p1 : p0;
-    const float c2 = bit ? p2 : p1;
-    lo1 = pos ? mid : c2;
-    hi1 = pos ? c2 : mid;
-    return make_float2(pos ? c0 : mid, pos ? mid : c0);  // (lo0, hi0)
-}
-
-__device__ __forceinline__ ChildSlabs descend_slabs(const ChildSlabs& p, uint32_t k, V3 origin_c, float s_c, V3 rrd,
-                                                    V3 bias) {
-    ChildSlabs c;
-    const float mx = (origin_c.x + s_c) * rrd.x - bias.x;
-    const float my = (origin_c.y + s_c) * rrd.y - bias.y;
-    const float mz = (origin_c.z + s_c) * rrd.z - bias.z;
-    float2 v = child_axis(p.xl0, p.xl1, p.xh0, p.xh1, rrd.x > 0.0f, k & 4u, mx, c.xl1, c.xh1);
-    c.xl0 = v.x;
-    c.xh0 = v.y;
-    v = child_axis(p.yl0, p.yl1, p.yh0, p.yh1, rrd.y > 0.0f, k & 2u, my, c.yl1, c.yh1);
-    c.yl0 = v.x;
-    c.yh0 = v.y;
-    v = child_axis(p.zl0, p.zl1, p.zh0, p.zh1, rrd.z > 0.0f, k & 1u, mz, c.zl1, c.zh1);
-    c.zl0 = v.x;
-    c.zh0 = v.y;
-    return c;
-}
-
 // fmaxf/fminf are exact and the slab values are finite (every ray direction
 // component is at least 2^-23 in magnitude), so the per-child max/min may be
 // grouped as max(max(x, y), z): the x-y part is shared by the two children
@@ -640,7 +603,7 @@ __device__ V3 trace_df_masked(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint3
         node = child;
         ++depth;
         side *= 0.5f;
-        slabs = descend_slabs(slabs, k, origin, side, rrd, bias);
+        slabs = child_slabs(origin, side, rrd, bias);
         mask = hit_mask(slabs);
         if (COUNT) loads += 8;
     }
@@ -1083,7 +1046,7 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
         node = child;
         ++depth;
         side *= 0.5f;
-        slabs = descend_slabs(slabs, k, origin, side, rrd, bias);
+        slabs = child_slabs(origin, side, rrd, bias);
         own = mine ? hit_mask(slabs) : 0u;
         if (COUNT && mine) loads += 8;
         uni = __reduce_or_sync(0xFFFFFFFFu, own);
