@@ -1011,22 +1011,29 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
             slabs = child_slabs(origin, side, rrd, bias);
             continue;
         }
-        const uint32_t k = __ffs(uni) - 1;
-        uni &= uni - 1;
-        const bool mine = (own >> k) & 1u;
-        own &= ~(1u << k);
-        const uint32_t child = a.child(node, k);
-        if (COUNT && mine) ++loads;
-        if (a.is_leaf(child)) {
-            if (mine) {
+        uint32_t k = __ffs(uni) - 1;
+        uint32_t child = a.child(node, k);
+        // a run of leaf children (at most 8): accumulated in index order
+        // without returning to the loop head
+        while (a.is_leaf(child)) {
+            uni &= uni - 1;
+            if ((own >> k) & 1u) {
+                own &= ~(1u << k);
                 float t0, t1;
                 child_span(slabs, k, t0, t1);
                 const V3 color = leaf_rgb(a.color(child));
-                if (COUNT) ++loads;
+                if (COUNT) loads += 2;  // the child's is_leaf_depth and colour
                 total = total + color * (t1 - fmaxf(t0, 0.0f));
             }
-            continue;
+            if (uni == 0) break;
+            k = __ffs(uni) - 1;
+            child = a.child(node, k);
         }
+        if (uni == 0 || a.is_leaf(child)) continue;
+        uni &= uni - 1;
+        const bool mine = (own >> k) & 1u;
+        own &= ~(1u << k);
+        if (COUNT && mine) ++loads;
         // descend into child k (lanes that miss it sit out its subtree)
         if (uni != 0) {
             if (sp >= STACK_DEPTH) {
