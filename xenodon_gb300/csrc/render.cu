@@ -945,19 +945,24 @@ struct PacketStacksWarp {
     uint32_t* w_state;
     uint8_t* l_mask;
     uint32_t lane;
+    float* w_origin;  // 3 per entry
     __device__ __forceinline__ uint32_t& node(int i) { return w_node[i]; }
     __device__ __forceinline__ uint32_t& state(int i) { return w_state[i]; }
+    __device__ __forceinline__ float& origin(int i, int axis) { return w_origin[i * 3 + axis]; }
     __device__ __forceinline__ uint32_t mask(int i) const { return l_mask[i * 32 + lane]; }
     __device__ __forceinline__ void set_mask(int i, uint32_t m) { l_mask[i * 32 + lane] = (uint8_t)m; }
 };
 
 struct PacketStacksColumns {
-    uint32_t* node0;   // lane 0's first column
+    uint32_t* node0;   // lane 0's first column (lanes 1..4: state, origin x, y, z)
     uint32_t* state0;  // lane 1's first column
     uint32_t* mine;    // this lane's second column
     uint32_t stride;
     __device__ __forceinline__ uint32_t& node(int i) { return node0[i * stride]; }
     __device__ __forceinline__ uint32_t& state(int i) { return state0[i * stride]; }
+    __device__ __forceinline__ float& origin(int i, int axis) {
+        return reinterpret_cast<float*>(node0 + 2 + axis)[i * stride];
+    }
     __device__ __forceinline__ uint32_t mask(int i) const { return mine[i * stride]; }
     __device__ __forceinline__ void set_mask(int i, uint32_t m) { mine[i * stride] = m; }
 };
@@ -993,21 +998,12 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
             uni = st & 0xFFu;
             depth = st >> 8;
             own = ps.mask(sp);
-            float s2, inv;
-            bool ex;
-            if (depth <= 124u) {
-                s2 = __uint_as_float((127u - depth) << 23);
-                inv = __uint_as_float((127u + depth) << 23);
-                side = s2 * 0.5f;
-                ex = true;
-            } else {
-                side = ldexpf(1.0f, -(int)(depth > 1000u ? 1000u : depth)) * 0.5f;
-                s2 = side * 2.0f;
-                inv = __frcp_rn(s2);
-                ex = pow2_with_normal_reciprocal(s2);
-            }
-            origin = origin - v3(gl_mod_pow2(origin.x, s2, inv, ex), gl_mod_pow2(origin.y, s2, inv, ex),
-                                 gl_mod_pow2(origin.z, s2, inv, ex));
+            // the reference recomputes the node's origin as pos - mod(pos,
+            // 2 side) from the depth field; with consistent depth fields that
+            // is the origin stored when the node was pushed, bit for bit
+            side = depth <= 124u ? __uint_as_float((126u - depth) << 23)
+                                 : ldexpf(1.0f, -(int)(depth > 1000u ? 1000u : depth)) * 0.5f;
+            origin = v3(ps.origin(sp, 0), ps.origin(sp, 1), ps.origin(sp, 2));
             slabs = child_slabs(origin, side, rrd, bias);
             continue;
         }
@@ -1043,6 +1039,9 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
             if (lane == 0) {
                 ps.node(sp) = node;
                 ps.state(sp) = uni | (depth << 8);
+                ps.origin(sp, 0) = origin.x;
+                ps.origin(sp, 1) = origin.y;
+                ps.origin(sp, 2) = origin.z;
             }
             ps.set_mask(sp, own);
             ++sp;
@@ -1067,6 +1066,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) df_packet_kernel(Frame f, Acc a
     __shared__ uint32_t s_node[(BLOCK_THREADS / 32) * STACK_DEPTH];
     __shared__ uint32_t s_state[(BLOCK_THREADS / 32) * STACK_DEPTH];
     __shared__ uint8_t s_mask[(BLOCK_THREADS / 32) * STACK_DEPTH * 32];
+    __shared__ float s_origin[(BLOCK_THREADS / 32) * STACK_DEPTH * 3];
     fill_unorm_lut();
     const uint32_t warp = threadIdx.x >> 5;
     uint32_t ix, iy;
@@ -1074,7 +1074,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) df_packet_kernel(Frame f, Acc a
     const V3 rd = primary_ray(f, active ? ix : 0u, active ? iy : 0u);
     uint32_t loads = 0, err = 0;
     PacketStacksWarp ps{s_node + warp * STACK_DEPTH, s_state + warp * STACK_DEPTH, s_mask + warp * STACK_DEPTH * 32,
-                        threadIdx.x & 31u};
+                        threadIdx.x & 31u, s_origin + warp * STACK_DEPTH * 3};
     const V3 total = trace_df_packet<COUNT>(a, f.translation, rd, active, loads, err, ps);
     if (active) write_outputs(f, o, ix, iy, total * voxel_emission_coeff(f, rd), loads, err);
 }
