@@ -969,7 +969,6 @@ struct PacketStacksColumns {
 
 template <bool COUNT, class Acc, class PS>
 __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t& loads, uint32_t& err, PS& ps) {
-    const uint32_t lane = threadIdx.x & 31u;
     const V3 rrd = vs(1.0f) / rd;
     const V3 bias = rrd * ro;
     int sp = 0;
@@ -1036,13 +1035,13 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
                 if (active) err |= 2u;
                 break;
             }
-            if (lane == 0) {
-                ps.node(sp) = node;
-                ps.state(sp) = uni | (depth << 8);
-                ps.origin(sp, 0) = origin.x;
-                ps.origin(sp, 1) = origin.y;
-                ps.origin(sp, 2) = origin.z;
-            }
+            // every lane holds the same node, masks union, depth and origin
+            // and writes them itself, so its later reads see its own writes
+            ps.node(sp) = node;
+            ps.state(sp) = uni | (depth << 8);
+            ps.origin(sp, 0) = origin.x;
+            ps.origin(sp, 1) = origin.y;
+            ps.origin(sp, 2) = origin.z;
             ps.set_mask(sp, own);
             ++sp;
         }
@@ -1056,7 +1055,6 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
         own = mine ? hit_mask(slabs) : 0u;
         if (COUNT && mine) loads += 8;
         uni = __reduce_or_sync(0xFFFFFFFFu, own);
-        __syncwarp();
     }
     return total;
 }
