@@ -347,20 +347,3 @@ def test_dda_raw_texel_reads_equal_normalized(ctx, blob_volumes, monkeypatch, ca
     raw_vol = ctx.upload_grid(g)
     b, _ = check_parity(ctx, "dda", CAMS[cam], p, v, grid=g, vol=raw_vol, label=f"dda-raw/{cam}")
     assert np.array_equal(a, b)
-
-
-@pytest.mark.parametrize("cam", ["oblique", "inside", "grazing", "front"])
-def test_esvo_while_while_loop_equals_one_loop(ctx, blob_volumes, monkeypatch, cam):
-    # XN_ESVO_LOOP=ww: descents run in an inner loop; per ray the same steps
-    import xenodon_gb300 as xg
-    _, nodes, side = blob_volumes
-    vol = ctx.upload_svo(nodes, side)
-    p, v = _params_pair(xg, 85, 47)
-    monkeypatch.setenv("XN_ESVO_LOOP", "ww")
-    ww, _ = check_parity(ctx, "esvo", CAMS[cam], p, v, nodes=nodes, vol=vol, label=f"esvo-ww/{cam}")
-    _, em_w, loads_w = _gpu_counts(ctx, vol, "esvo", xg.make_camera(*CAMS[cam]), p)
-    monkeypatch.delenv("XN_ESVO_LOOP")
-    one, _, _ = ctx.render(vol, "esvo", xg.make_camera(*CAMS[cam]), p)
-    _, em_1, loads_1 = _gpu_counts(ctx, vol, "esvo", xg.make_camera(*CAMS[cam]), p)
-    assert np.array_equal(ww, one)
-    assert np.array_equal(em_w, em_1) and np.array_equal(loads_w, loads_1)

@@ -485,9 +485,6 @@ int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_p
         // masked svo-df walked by the whole warp unless XN_DF_PACKET=0
         const char* pk = std::getenv("XN_DF_PACKET");
         L.df_packet = !(pk && pk[0] == '0');
-        // esvo's loop: while-while with XN_ESVO_LOOP=ww
-        const char* el = std::getenv("XN_ESVO_LOOP");
-        L.esvo_ww = el && std::strcmp(el, "ww") == 0;
     }
     for (int i = 0; i < 3; ++i) L.dim[i] = v->dim[i];
     return XN_OK;

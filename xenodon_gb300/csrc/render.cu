@@ -719,119 +719,6 @@ __device__ V3 trace_esvo(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& 
     return total;
 }
 
-template <bool COUNT, class Acc, class Stacks = LocalStacks>
-__device__ V3 trace_esvo_ww(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& err, Stacks* shared_stacks = nullptr) {
-    const uint32_t depth = STACK_DEPTH;
-    Stacks local;
-    Stacks& stk = shared_stacks ? *shared_stacks : local;  // first: parent, second: t_max bits
-#pragma unroll
-    for (int i = 0; i < STACK_DEPTH; ++i) { stk.first(i) = 0; stk.second(i) = 0u; }
-
-    V3 t_coeff = v3(1.0f / -fabsf(rd.x), 1.0f / -fabsf(rd.y), 1.0f / -fabsf(rd.z));
-    V3 t_bias = t_coeff * ro;
-    bool gx = rd.x > 0.0f, gy = rd.y > 0.0f, gz = rd.z > 0.0f;
-    {
-        V3 alt = t_coeff * 3.0f - t_bias;
-        if (gx) t_bias.x = alt.x;
-        if (gy) t_bias.y = alt.y;
-        if (gz) t_bias.z = alt.z;
-    }
-    const uint32_t octant_mask = cxor(0u, gx, gy, gz);
-    float t_min = max_elem(t_coeff * 2.0f - t_bias);
-    float t_max = min_elem(t_coeff - t_bias);
-    float h = t_max;
-    t_min = fmaxf(t_min, 0.0f);
-    t_max = fminf(t_max, 1.73205078f);  // float(sqrt(3))
-
-    uint32_t parent = a.root();
-    uint32_t idx = 0;
-    V3 pos = vs(1.0f);
-    uint32_t scale = depth - 1;
-    float scale_exp2 = 0.5f;
-    {
-        V3 tc = t_coeff * 1.5f - t_bias;
-        bool ax = tc.x > t_min, ay = tc.y > t_min, az = tc.z > t_min;
-        if (ax) pos.x = 1.5f;
-        if (ay) pos.y = 1.5f;
-        if (az) pos.z = 1.5f;
-        idx = cxor(idx, ax, ay, az);
-    }
-    V3 total = vs(0.0f);
-    uint32_t iter = 0;
-    while (scale < depth) {
-        // while-while: descend as long as the child at idx is hit and
-        // internal (the lanes of a warp finish their descents together),
-        // then accumulate / advance / pop.  Per lane the same steps in the
-        // same order as the one-loop form.
-        V3 t_corner;
-        float tc_max;
-        bool stop = false;
-        for (;;) {
-            if (++iter > SVO_MAX_ITER) { err |= 1u; stop = true; break; }
-            t_corner = pos * t_coeff - t_bias;
-            tc_max = min_elem(t_corner);
-            if (!(t_min <= t_max)) break;
-            const float tv_max = fminf(t_max, tc_max);
-            if (!(t_min <= tv_max)) break;
-            {
-                uint32_t child = a.child(parent, idx ^ octant_mask);
-                if (COUNT) loads += 2;
-                if (a.is_leaf(child)) {
-                    V3 color = leaf_rgb(a.color(child));
-                    if (COUNT) ++loads;
-                    total = total + color * (tv_max - t_min);
-                    break;
-                } else {
-                    if (tc_max < h) {
-                        stk.first(scale) = parent;
-                        stk.second(scale) = __float_as_uint(t_max);
-                    }
-                    h = tc_max;
-                    parent = child;
-                    --scale;
-                    scale_exp2 *= 0.5f;
-                    V3 t_center = t_coeff * scale_exp2 + t_corner;
-                    bool ax = t_center.x > t_min, ay = t_center.y > t_min, az = t_center.z > t_min;
-                    idx = cxor(0u, ax, ay, az);
-                    if (ax) pos.x = pos.x + scale_exp2;
-                    if (ay) pos.y = pos.y + scale_exp2;
-                    if (az) pos.z = pos.z + scale_exp2;
-                    t_max = tv_max;
-                    continue;
-                }
-            }
-        }
-        if (stop) break;
-        // ADVANCE
-        bool ax = t_corner.x <= tc_max, ay = t_corner.y <= tc_max, az = t_corner.z <= tc_max;
-        uint32_t step_mask = cxor(0u, ax, ay, az);
-        if (ax) pos.x = pos.x - scale_exp2;
-        if (ay) pos.y = pos.y - scale_exp2;
-        if (az) pos.z = pos.z - scale_exp2;
-        t_min = tc_max;
-        idx ^= step_mask;
-        if ((idx & step_mask) != 0) {
-            // POP
-            uint32_t xx = __float_as_uint(pos.x) ^ __float_as_uint(pos.x + scale_exp2);
-            uint32_t xy = __float_as_uint(pos.y) ^ __float_as_uint(pos.y + scale_exp2);
-            uint32_t xz = __float_as_uint(pos.z) ^ __float_as_uint(pos.z + scale_exp2);
-            uint32_t dbits = (ax ? xx : 0u) | (ay ? xy : 0u) | (az ? xz : 0u);
-            scale = (__float_as_uint(__uint2float_rn(dbits)) >> 23) - 127u;
-            if (scale >= depth) break;  // the loop condition ends the ray
-            scale_exp2 = __uint_as_float((scale - depth + 127u) << 23);
-            parent = stk.first(scale);
-            t_max = __uint_as_float(stk.second(scale));
-            uint32_t shx = __float_as_uint(pos.x) >> scale;
-            uint32_t shy = __float_as_uint(pos.y) >> scale;
-            uint32_t shz = __float_as_uint(pos.z) >> scale;
-            pos = v3(__uint_as_float(shx << scale), __uint_as_float(shy << scale), __uint_as_float(shz << scale));
-            idx = (shx & 1u) * 4u + (shy & 1u) * 2u + (shz & 1u);
-            h = 0.0f;
-        }
-    }
-    return total;
-}
-
 // resources/svo_rope.comp:29-48
 template <bool COUNT, class Acc>
 __device__ __forceinline__ uint32_t find_relative(const Acc& a, uint32_t parent, V3 offset, V3 pos, V3& base,
@@ -1208,15 +1095,12 @@ __global__ void __launch_bounds__(SHARED_BLOCK) shared_stack_kernel(Frame f, Acc
     const V3 rd = primary_ray(f, ix, iy);
     uint32_t loads = 0, err = 0;
     V3 total;
-    if constexpr (TRAV == XN_TRAV_ESVO || TRAV == XN_TRAV_ESVO_WW) {
+    if constexpr (TRAV == XN_TRAV_ESVO) {
         // resources/esvo.comp:148-152
         V3 ro = f.translation + vs(1.0f);
         const float t0 = aabb_entry(vs(1.0f), vs(2.0f), ro, rd);
         ro = ro + rd * fmaxf(t0, 0.0f);
-        if constexpr (TRAV == XN_TRAV_ESVO_WW)
-            total = trace_esvo_ww<COUNT, Acc, SharedStacks>(a, ro, rd, loads, err, &stk);
-        else
-            total = trace_esvo<COUNT, Acc, SharedStacks>(a, ro, rd, loads, err, &stk);
+        total = trace_esvo<COUNT, Acc, SharedStacks>(a, ro, rd, loads, err, &stk);
     } else {
         total = trace_df_masked<COUNT, Acc, SharedStacks>(a, f.translation, rd, loads, err, &stk);
     }
@@ -1276,17 +1160,6 @@ cudaError_t launch_render(const RenderLaunch& L, cudaStream_t stream) {
                   (uint64_t)L.dim[0] * L.dim[1]};
         if (count) dda_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, g, o);
         else dda_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, g, o);
-    } else if (L.traversal == XN_TRAV_ESVO && L.shared_stacks && L.esvo_ww) {
-        const dim3 grid16((L.out_w + 15) / 16, (L.out_h + SHARED_BLOCK / 16 - 1) / (SHARED_BLOCK / 16));
-        if (L.layout == XN_LAYOUT_REFERENCE) {
-            const RefNodes acc{static_cast<const uint32_t*>(L.nodes)};
-            if (count) shared_stack_kernel<XN_TRAV_ESVO_WW, true><<<grid16, SHARED_BLOCK, 0, stream>>>(f, acc, o);
-            else shared_stack_kernel<XN_TRAV_ESVO_WW, false><<<grid16, SHARED_BLOCK, 0, stream>>>(f, acc, o);
-        } else {
-            const CompactNodes acc{L.inner, L.inner_depth};
-            if (count) shared_stack_kernel<XN_TRAV_ESVO_WW, true><<<grid16, SHARED_BLOCK, 0, stream>>>(f, acc, o);
-            else shared_stack_kernel<XN_TRAV_ESVO_WW, false><<<grid16, SHARED_BLOCK, 0, stream>>>(f, acc, o);
-        }
     } else if (L.traversal == XN_TRAV_ESVO && L.shared_stacks) {
         const dim3 grid16((L.out_w + 15) / 16, (L.out_h + SHARED_BLOCK / 16 - 1) / (SHARED_BLOCK / 16));
         if (L.layout == XN_LAYOUT_REFERENCE) {

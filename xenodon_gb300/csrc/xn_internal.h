@@ -18,8 +18,7 @@ enum {
     XN_TRAV_SVO_DF = 3,
     XN_TRAV_SVO_ROPE = 4,
     XN_TRAV_SVO_DF_MASKED = 5,  // svo-df on an octree with consistent depth fields (render.cu)
-    XN_TRAV_SVO_NAIVE_ROOT = 6,  // svo-naive with every find from the root
-    XN_TRAV_ESVO_WW = 7          // esvo with the while-while loop (render.cu)
+    XN_TRAV_SVO_NAIVE_ROOT = 6  // svo-naive with every find from the root
 };
 
 // Everything one traversal launch needs; built by the C-ABI layer from an
@@ -50,7 +49,6 @@ struct RenderLaunch {
     int shared_stacks;            // esvo and masked svo-df with their stacks in shared memory
     int naive_resume;             // svo-naive's find resumes from the previous step's path
     int df_packet;                // masked svo-df walked by the whole warp (df_packet_kernel)
-    int esvo_ww;                  // esvo's loop in the while-while form
     // outputs (device pointers)
     void* d_rgba;
     float* d_emission;
