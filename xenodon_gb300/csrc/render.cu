@@ -487,12 +487,16 @@ __device__ __forceinline__ ChildSlabs child_slabs(V3 origin, float s, V3 rrd, V3
     const float x0 = origin.x * rrd.x - bias.x, x1 = px1 * rrd.x - bias.x, x2 = (px1 + s) * rrd.x - bias.x;
     const float y0 = origin.y * rrd.y - bias.y, y1 = py1 * rrd.y - bias.y, y2 = (py1 + s) * rrd.y - bias.y;
     const float z0 = origin.z * rrd.z - bias.z, z1 = pz1 * rrd.z - bias.z, z2 = (pz1 + s) * rrd.z - bias.z;
-    return ChildSlabs{fminf(x0, x1), fminf(x1, x2), fmaxf(x0, x1), fmaxf(x1, x2),
+    // the x entry slabs are clamped at 0: every use of a child's t_min is
+    // max(t_min, 0) (the leaf's step, and the hit test t_min < t_max &&
+    // t_max > 0, which is max(t_min, 0) < t_max), and fmaxf is exact and
+    // associative on these finite values
+    return ChildSlabs{fmaxf(fminf(x0, x1), 0.0f), fmaxf(fminf(x1, x2), 0.0f), fmaxf(x0, x1), fmaxf(x1, x2),
                       fminf(y0, y1), fminf(y1, y2), fmaxf(y0, y1), fmaxf(y1, y2),
                       fminf(z0, z1), fminf(z1, z2), fmaxf(z0, z1), fmaxf(z1, z2)};
 }
 
-// t_min / t_max of child k, as the reference computes them for that box
+// max(t_min, 0) / t_max of child k, as the reference computes them for that box
 __device__ __forceinline__ void child_span(const ChildSlabs& c, uint32_t k, float& t0, float& t1) {
     const bool bx = k & 4u, by = k & 2u, bz = k & 1u;
     t0 = fmaxf(bx ? c.xl1 : c.xl0, fmaxf(by ? c.yl1 : c.yl0, bz ? c.zl1 : c.zl0));
@@ -514,7 +518,7 @@ __device__ __forceinline__ uint32_t hit_mask(const ChildSlabs& c) {
         for (uint32_t bz = 0; bz < 2; ++bz) {
             const float t0 = fmaxf(lo, bz ? c.zl1 : c.zl0);
             const float t1 = fminf(hi, bz ? c.zh1 : c.zh0);
-            if (t0 < t1 && t1 > 0.0f) m |= 1u << (xy * 2u + bz);
+            if (t0 < t1) m |= 1u << (xy * 2u + bz);  // t0 >= 0: t_max > 0 follows
         }
     }
     return m;
@@ -588,7 +592,7 @@ __device__ V3 trace_df_masked(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint3
         if (a.is_leaf(child)) {
             const V3 color = leaf_rgb(a.color(child));
             if (COUNT) ++loads;
-            total = total + color * (t1 - fmaxf(t0, 0.0f));
+            total = total + color * (t1 - t0);
             continue;
         }
         // descend into child k; the reference pushes unless k == 7
@@ -1018,7 +1022,7 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
                 child_span(slabs, k, t0, t1);
                 const V3 color = leaf_rgb(a.color(child));
                 if (COUNT) loads += 2;  // the child's is_leaf_depth and colour
-                total = total + color * (t1 - fmaxf(t0, 0.0f));
+                total = total + color * (t1 - t0);
             }
             if (uni == 0) break;
             k = __ffs(uni) - 1;
