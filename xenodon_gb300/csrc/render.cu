@@ -938,34 +938,54 @@ __global__ void __launch_bounds__(BLOCK_THREADS) svo_kernel(Frame f, Acc a, Outp
 // order with the same arithmetic, so every ray's result (and its word count)
 // is the one-ray-per-thread result, while the control flow, the node loads
 // (one address per warp) and the pops are shared by the warp.
-//   w_node / w_state: the warp's stack (node, union of remaining masks |
-//   depth << 8); l_mask: each lane's remaining mask per stack entry.
-// The warp's stacks for trace_df_packet: contiguous per-warp arrays (its own
-// kernel) or, in the batch kernel, carved from the per-thread columns of the
-// shared stacks (warp stack in lanes 0 and 1's first columns, each lane's
-// masks in its own second column), so they never overlap another warp's.
+//   each stack entry: the node, the union of the lanes' remaining masks, the
+//   node's origin and child size (all warp-uniform), and each lane's own
+//   remaining mask.
+// The warp's stacks for trace_df_packet: per-warp arrays (its own kernel; the
+// uniform part as one 8-byte and one 16-byte word per entry) or, in the batch
+// kernel, carved from the per-thread columns of the shared stacks (the
+// uniform words in lanes 0..5's first columns, each lane's masks in its own
+// second column), so they never overlap another warp's.
 struct PacketStacksWarp {
-    uint32_t* w_node;
-    uint32_t* w_state;
+    uint2* w_ns;     // node, union mask
+    float4* w_geo;   // origin x, y, z, child size
     uint8_t* l_mask;
     uint32_t lane;
-    float* w_origin;  // 3 per entry
-    __device__ __forceinline__ uint32_t& node(int i) { return w_node[i]; }
-    __device__ __forceinline__ uint32_t& state(int i) { return w_state[i]; }
-    __device__ __forceinline__ float& origin(int i, int axis) { return w_origin[i * 3 + axis]; }
+    __device__ __forceinline__ void push(int i, uint32_t node, uint32_t uni, V3 o, float side) {
+        w_ns[i] = make_uint2(node, uni);
+        w_geo[i] = make_float4(o.x, o.y, o.z, side);
+    }
+    __device__ __forceinline__ void pop(int i, uint32_t& node, uint32_t& uni, V3& o, float& side) const {
+        const uint2 ns = w_ns[i];
+        const float4 g = w_geo[i];
+        node = ns.x;
+        uni = ns.y;
+        o = v3(g.x, g.y, g.z);
+        side = g.w;
+    }
     __device__ __forceinline__ uint32_t mask(int i) const { return l_mask[i * 32 + lane]; }
     __device__ __forceinline__ void set_mask(int i, uint32_t m) { l_mask[i * 32 + lane] = (uint8_t)m; }
 };
 
 struct PacketStacksColumns {
-    uint32_t* node0;   // lane 0's first column (lanes 1..4: state, origin x, y, z)
-    uint32_t* state0;  // lane 1's first column
-    uint32_t* mine;    // this lane's second column
+    uint32_t* w0;    // lane 0's first column (lanes 0..5: node, union mask, origin x, y, z, child size)
+    uint32_t* mine;  // this lane's second column
     uint32_t stride;
-    __device__ __forceinline__ uint32_t& node(int i) { return node0[i * stride]; }
-    __device__ __forceinline__ uint32_t& state(int i) { return state0[i * stride]; }
-    __device__ __forceinline__ float& origin(int i, int axis) {
-        return reinterpret_cast<float*>(node0 + 2 + axis)[i * stride];
+    __device__ __forceinline__ void push(int i, uint32_t node, uint32_t uni, V3 o, float side) {
+        uint32_t* e = w0 + (size_t)i * stride;
+        e[0] = node;
+        e[1] = uni;
+        e[2] = __float_as_uint(o.x);
+        e[3] = __float_as_uint(o.y);
+        e[4] = __float_as_uint(o.z);
+        e[5] = __float_as_uint(side);
+    }
+    __device__ __forceinline__ void pop(int i, uint32_t& node, uint32_t& uni, V3& o, float& side) const {
+        const uint32_t* e = w0 + (size_t)i * stride;
+        node = e[0];
+        uni = e[1];
+        o = v3(__uint_as_float(e[2]), __uint_as_float(e[3]), __uint_as_float(e[4]));
+        side = __uint_as_float(e[5]);
     }
     __device__ __forceinline__ uint32_t mask(int i) const { return mine[i * stride]; }
     __device__ __forceinline__ void set_mask(int i, uint32_t m) { mine[i * stride] = m; }
@@ -977,7 +997,6 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
     const V3 bias = rrd * ro;
     int sp = 0;
     uint32_t node = a.root();
-    uint32_t depth = 0;
     V3 origin = vs(0.0f);
     float side = 0.5f;
     V3 total = vs(0.0f);
@@ -996,17 +1015,12 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
             // parent's depth; masked svo-df takes it from the stack)
             --sp;
             if (sp < 0) break;
-            node = ps.node(sp);
-            const uint32_t st = ps.state(sp);
-            uni = st & 0xFFu;
-            depth = st >> 8;
+            // the reference recomputes the node's child size from its depth
+            // field and its origin as pos - mod(pos, 2 side); with consistent
+            // depth fields those are the values stored when the node was
+            // pushed, bit for bit
+            ps.pop(sp, node, uni, origin, side);
             own = ps.mask(sp);
-            // the reference recomputes the node's origin as pos - mod(pos,
-            // 2 side) from the depth field; with consistent depth fields that
-            // is the origin stored when the node was pushed, bit for bit
-            side = depth <= 124u ? __uint_as_float((126u - depth) << 23)
-                                 : ldexpf(1.0f, -(int)(depth > 1000u ? 1000u : depth)) * 0.5f;
-            origin = v3(ps.origin(sp, 0), ps.origin(sp, 1), ps.origin(sp, 2));
             slabs = child_slabs(origin, side, rrd, bias);
             continue;
         }
@@ -1039,13 +1053,9 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
                 if (active) err |= 2u;
                 break;
             }
-            // every lane holds the same node, masks union, depth and origin
+            // every lane holds the same node, masks union, origin and size
             // and writes them itself, so its later reads see its own writes
-            ps.node(sp) = node;
-            ps.state(sp) = uni | (depth << 8);
-            ps.origin(sp, 0) = origin.x;
-            ps.origin(sp, 1) = origin.y;
-            ps.origin(sp, 2) = origin.z;
+            ps.push(sp, node, uni, origin, side);
             ps.set_mask(sp, own);
             ++sp;
         }
@@ -1053,7 +1063,6 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
         origin = v3(origin.x + ((k & 4u) ? side : 0.0f), origin.y + ((k & 2u) ? side : 0.0f),
                     origin.z + ((k & 1u) ? side : 0.0f));
         node = child;
-        ++depth;
         side *= 0.5f;
         slabs = child_slabs(origin, side, rrd, bias);
         own = mine ? hit_mask(slabs) : 0u;
@@ -1065,18 +1074,17 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
 
 template <bool COUNT, class Acc>
 __global__ void __launch_bounds__(BLOCK_THREADS) df_packet_kernel(Frame f, Acc a, Outputs o) {
-    __shared__ uint32_t s_node[(BLOCK_THREADS / 32) * STACK_DEPTH];
-    __shared__ uint32_t s_state[(BLOCK_THREADS / 32) * STACK_DEPTH];
+    __shared__ float4 s_geo[(BLOCK_THREADS / 32) * STACK_DEPTH];
+    __shared__ uint2 s_ns[(BLOCK_THREADS / 32) * STACK_DEPTH];
     __shared__ uint8_t s_mask[(BLOCK_THREADS / 32) * STACK_DEPTH * 32];
-    __shared__ float s_origin[(BLOCK_THREADS / 32) * STACK_DEPTH * 3];
     fill_unorm_lut();
     const uint32_t warp = threadIdx.x >> 5;
     uint32_t ix, iy;
     const bool active = pixel_of_thread(f, ix, iy);
     const V3 rd = primary_ray(f, active ? ix : 0u, active ? iy : 0u);
     uint32_t loads = 0, err = 0;
-    PacketStacksWarp ps{s_node + warp * STACK_DEPTH, s_state + warp * STACK_DEPTH, s_mask + warp * STACK_DEPTH * 32,
-                        threadIdx.x & 31u, s_origin + warp * STACK_DEPTH * 3};
+    PacketStacksWarp ps{s_ns + warp * STACK_DEPTH, s_geo + warp * STACK_DEPTH, s_mask + warp * STACK_DEPTH * 32,
+                        threadIdx.x & 31u};
     const V3 total = trace_df_packet<COUNT>(a, f.translation, rd, active, loads, err, ps);
     if (active) write_outputs(f, o, ix, iy, total * voxel_emission_coeff(f, rd), loads, err);
 }
@@ -1356,7 +1364,7 @@ __device__ __forceinline__ uint32_t render_job_pixel_spec(const BatchJob& J, uin
         const Frame f = frame_of(J);
         const V3 rd = primary_ray(f, active ? ix : 0u, active ? iy : 0u);
         const uint32_t lane = threadIdx.x & 31u;
-        PacketStacksColumns ps{stk->a - lane, stk->a - lane + 1, stk->b, stk->stride};
+        PacketStacksColumns ps{stk->a - lane, stk->b, stk->stride};
         uint32_t loads = 0;
         const V3 total = trace_df_packet<false>(CompactNodes{J.inner, J.inner_depth}, f.translation, rd, active,
                                                 loads, err, ps);
