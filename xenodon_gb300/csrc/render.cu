@@ -997,6 +997,10 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
     const V3 bias = rrd * ro;
     int sp = 0;
     uint32_t node = a.root();
+    // the node is the same on every lane: lane j holds its child word j & 7,
+    // and a child word is a shuffle away
+    const uint32_t slot = threadIdx.x & 7u;
+    uint32_t words = a.child(node, slot);
     V3 origin = vs(0.0f);
     float side = 0.5f;
     V3 total = vs(0.0f);
@@ -1021,11 +1025,12 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
             // pushed, bit for bit
             ps.pop(sp, node, uni, origin, side);
             own = ps.mask(sp);
+            words = a.child(node, slot);
             slabs = child_slabs(origin, side, rrd, bias);
             continue;
         }
         uint32_t k = __ffs(uni) - 1;
-        uint32_t child = a.child(node, k);
+        uint32_t child = __shfl_sync(0xFFFFFFFFu, words, k);
         // a run of leaf children (at most 8): accumulated in index order
         // without returning to the loop head
         while (a.is_leaf(child)) {
@@ -1040,7 +1045,7 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
             }
             if (uni == 0) break;
             k = __ffs(uni) - 1;
-            child = a.child(node, k);
+            child = __shfl_sync(0xFFFFFFFFu, words, k);
         }
         if (uni == 0 || a.is_leaf(child)) continue;
         uni &= uni - 1;
@@ -1063,6 +1068,7 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
         origin = v3(origin.x + ((k & 4u) ? side : 0.0f), origin.y + ((k & 2u) ? side : 0.0f),
                     origin.z + ((k & 1u) ? side : 0.0f));
         node = child;
+        words = a.child(node, slot);
         side *= 0.5f;
         slabs = child_slabs(origin, side, rrd, bias);
         own = mine ? hit_mask(slabs) : 0u;
