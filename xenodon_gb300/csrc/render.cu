@@ -1008,17 +1008,20 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
     uint32_t own = active ? hit_mask(slabs) : 0u;
     if (COUNT && active) loads += 8;
     uint32_t uni = __reduce_or_sync(0xFFFFFFFFu, own);
-    uint32_t iter = 0;
+    // Between two pops the walk only descends, and after about 150 descents
+    // the child size is 0 and no child is hit; so a cap on the pops bounds
+    // the loop.
+    uint32_t pops = 0;
     for (;;) {
-        if (++iter > SVO_MAX_ITER) {
-            if (active) err |= 1u;
-            break;
-        }
         if (uni == 0) {
             // every lane is done with this node: pop (the reference reads the
             // parent's depth; masked svo-df takes it from the stack)
             --sp;
             if (sp < 0) break;
+            if (++pops > SVO_MAX_ITER) {
+                if (active) err |= 1u;
+                break;
+            }
             // the reference recomputes the node's child size from its depth
             // field and its origin as pos - mod(pos, 2 side); with consistent
             // depth fields those are the values stored when the node was
@@ -1032,17 +1035,17 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
         uint32_t k = __ffs(uni) - 1;
         uint32_t child = __shfl_sync(0xFFFFFFFFu, words, k);
         // a run of leaf children (at most 8): accumulated in index order
-        // without returning to the loop head
+        // without returning to the loop head.  A lane's mask bits below k are
+        // never read again, so they are left set.  A lane that missed the
+        // leaf adds color * 0 = +0, which leaves its sum (never -0) unchanged.
         while (a.is_leaf(child)) {
             uni &= uni - 1;
-            if ((own >> k) & 1u) {
-                own &= ~(1u << k);
-                float t0, t1;
-                child_span(slabs, k, t0, t1);
-                const V3 color = leaf_rgb(a.color(child));
-                if (COUNT) loads += 2;  // the child's is_leaf_depth and colour
-                total = total + color * (t1 - t0);
-            }
+            const bool hit = (own >> k) & 1u;
+            float t0, t1;
+            child_span(slabs, k, t0, t1);
+            const V3 color = leaf_rgb(a.color(child));
+            if (COUNT && hit) loads += 2;  // the child's is_leaf_depth and colour
+            total = total + color * (hit ? t1 - t0 : 0.0f);
             if (uni == 0) break;
             k = __ffs(uni) - 1;
             child = __shfl_sync(0xFFFFFFFFu, words, k);
@@ -1050,7 +1053,6 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
         if (uni == 0 || a.is_leaf(child)) continue;
         uni &= uni - 1;
         const bool mine = (own >> k) & 1u;
-        own &= ~(1u << k);
         if (COUNT && mine) ++loads;
         // descend into child k (lanes that miss it sit out its subtree)
         if (uni != 0) {
