@@ -247,12 +247,20 @@ __device__ __forceinline__ uint32_t find(const Acc& a, V3 pos, V3& base, float& 
 // descent can restart at the deepest node of the last path whose region holds
 // p, with the same offsets and extents, and reach the same leaf with the same
 // base and side.  The reference's word reads are still 2 per level + 1.
-constexpr int PATH_CACHE = 32;
+// The descent path of the last find: its nodes below the root (levels 1 ..
+// FIX_DEPTH, in local memory or a column of shared memory) and the scalars,
+// kept apart so that the scalars can stay in registers.
+constexpr int FIX_BITS = 30;
+constexpr int FIX_DEPTH = 24;
 
-// The descent path of the last find: its nodes (an array, in local memory)
-// and the scalars, kept apart so that the scalars can stay in registers.
-struct FindPathNodes {
-    uint32_t node[PATH_CACHE];
+struct LocalPath {
+    uint32_t n[FIX_DEPTH];
+    __device__ __forceinline__ uint32_t& node(int level) { return n[level - 1]; }
+};
+struct SharedPath {
+    uint32_t* base;  // this thread's column
+    uint32_t stride;
+    __device__ __forceinline__ uint32_t& node(int level) { return base[(level - 1) * stride]; }
 };
 struct FindPath {
     int depth = -1;          // depth of the last leaf found, -1: none (or too deep to cache)
@@ -266,8 +274,6 @@ struct FindPath {
 // -inf/+inf where it is the root's) holds p exactly when the top j bits of
 // the integer equal O's: the clamp supplies the open bounds.  Origins and
 // extents of depth <= 24 are exact floats either way.
-constexpr int FIX_BITS = 30;
-constexpr int FIX_DEPTH = 24;
 
 __device__ __forceinline__ uint32_t fix_coord(float p) {
     // floor(p * 2^30) (the scaling is exact); the conversion saturates and
@@ -278,8 +284,8 @@ __device__ __forceinline__ uint32_t fix_coord(float p) {
 
 __device__ __forceinline__ float fix_to_float(uint32_t v) { return (float)v * (1.0f / 1073741824.0f); }
 
-template <bool COUNT, class Acc>
-__device__ __forceinline__ uint32_t find_cached(const Acc& a, FindPath& path, FindPathNodes& pn, V3 pos, V3& base,
+template <bool COUNT, class Acc, class Path>
+__device__ __forceinline__ uint32_t find_cached(const Acc& a, FindPath& path, Path& pn, V3 pos, V3& base,
                                                 float& side, uint32_t& loads, uint32_t& err) {
     const uint32_t px = fix_coord(pos.x), py = fix_coord(pos.y), pz = fix_coord(pos.z);
     int level = 0;
@@ -292,15 +298,16 @@ __device__ __forceinline__ uint32_t find_cached(const Acc& a, FindPath& path, Fi
         if (j > path.depth) j = path.depth;
         if (j >= 1) {
             level = j;
-            index = pn.node[j];
+            index = pn.node(j);
         }
     }
+    // the path's levels up to the resumed one are already in place
     for (;; ++level) {
-        if (level < PATH_CACHE) pn.node[level] = index;
         if (a.is_leaf(index) || level == FIX_DEPTH) break;
         const int b = FIX_BITS - 1 - level;
         const uint32_t k = (((px >> b) & 1u) << 2) | (((py >> b) & 1u) << 1) | ((pz >> b) & 1u);
         index = a.child(index, k);
+        pn.node(level + 1) = index;
     }
     const uint32_t keep = ~((1u << (FIX_BITS - level)) - 1u);
     V3 offset = v3(fix_to_float(px & keep), fix_to_float(py & keep), fix_to_float(pz & keep));
@@ -309,7 +316,6 @@ __device__ __forceinline__ uint32_t find_cached(const Acc& a, FindPath& path, Fi
         // below depth 24 (deeper than any grid of 2^24 voxels per axis): the
         // reference's float descent
         for (;; ++level) {
-            if (level < PATH_CACHE) pn.node[level] = index;
             if (a.is_leaf(index)) break;
             if (level >= FIND_MAX_DEPTH) {
                 err |= 1u;
@@ -328,7 +334,7 @@ __device__ __forceinline__ uint32_t find_cached(const Acc& a, FindPath& path, Fi
     base = offset;
     side = extent;
     if (COUNT) loads += 2u * (uint32_t)level + 1u;
-    if (level <= FIX_DEPTH && level < PATH_CACHE) {
+    if (level <= FIX_DEPTH) {
         path.depth = level;
         path.cx = px & keep;
         path.cy = py & keep;
@@ -342,8 +348,8 @@ __device__ __forceinline__ uint32_t find_cached(const Acc& a, FindPath& path, Fi
 // resources/svo_naive.comp:29-71.  RESUME: each step's find resumes from the
 // previous path (find_cached); else it descends from the root (find), as the
 // reference does.  Both find the same node with the same base and side.
-template <bool COUNT, class Acc, bool RESUME = true>
-__device__ V3 trace_naive(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& err) {
+template <bool COUNT, class Acc, bool RESUME = true, class Path = LocalPath>
+__device__ V3 trace_naive(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& err, Path* shared_path = nullptr) {
     const float MIN_STEP = 0.00001f;
     V3 rrd = vs(1.0f) / rd;
     V3 bias = rrd * ro;
@@ -357,7 +363,8 @@ __device__ V3 trace_naive(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t&
     float t = t_min + MIN_STEP;
     uint32_t iter = 0;
     FindPath path;
-    FindPathNodes pn;
+    Path local;
+    Path& pn = shared_path ? *shared_path : local;
     while (t < t_max) {
         if (++iter > SVO_MAX_ITER) { err |= 1u; break; }
         V3 p = rd * t + ro;
@@ -913,8 +920,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS) svo_kernel(Frame f, Acc a, Outp
         float t0 = aabb_entry(vs(1.0f), vs(2.0f), ro, rd);
         ro = ro + rd * fmaxf(t0, 0.0f);
         total = trace_esvo<COUNT>(a, ro, rd, loads, err);
-    } else if (TRAV == XN_TRAV_SVO_NAIVE) {
-        total = trace_naive<COUNT>(a, f.translation, rd, loads, err);
+    } else if constexpr (TRAV == XN_TRAV_SVO_NAIVE) {
+        // the find's path nodes in a column of shared memory (12 KB per block)
+        __shared__ uint32_t s_path[FIX_DEPTH * BLOCK_THREADS];
+        SharedPath sp{s_path + threadIdx.x, BLOCK_THREADS};
+        total = trace_naive<COUNT, Acc, true, SharedPath>(a, f.translation, rd, loads, err, &sp);
     } else if (TRAV == XN_TRAV_SVO_NAIVE_ROOT) {
         total = trace_naive<COUNT, Acc, false>(a, f.translation, rd, loads, err);
     } else if (TRAV == XN_TRAV_SVO_DF) {
