@@ -1011,6 +1011,8 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
     // and a child word is a shuffle away
     const uint32_t slot = threadIdx.x & 7u;
     uint32_t words = a.child(node, slot);
+    // which of the node's children are leaves: lanes 0..7 hold words 0..7
+    uint32_t leaves = __ballot_sync(0xFFFFFFFFu, a.is_leaf(words)) & 0xFFu;
     V3 origin = vs(0.0f);
     float side = 0.5f;
     V3 total = vs(0.0f);
@@ -1039,32 +1041,42 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
             ps.pop(sp, node, uni, origin, side);
             own = ps.mask(sp);
             words = a.child(node, slot);
+            leaves = __ballot_sync(0xFFFFFFFFu, a.is_leaf(words)) & 0xFFu;
             slabs = child_slabs(origin, side, rrd, bias);
             continue;
         }
-        uint32_t k = __ffs(uni) - 1;
-        uint32_t child = __shfl_sync(0xFFFFFFFFu, words, k);
-        // a run of leaf children (at most 8): accumulated in index order
-        // without returning to the loop head.  A lane's mask bits below k are
-        // never read again, so they are left set.  A lane that missed the
-        // leaf adds color * 0 = +0, which leaves its sum (never -0) unchanged.
-        while (a.is_leaf(child)) {
-            uni &= uni - 1;
-            const bool hit = (own >> k) & 1u;
-            float t0, t1;
-            child_span(slabs, k, t0, t1);
-            const V3 color = leaf_rgb(a.color(child));
-            if (COUNT && hit) loads += 2;  // the child's is_leaf_depth and colour
-            total = total + color * (hit ? t1 - t0 : 0.0f);
-            if (uni == 0) break;
-            k = __ffs(uni) - 1;
-            child = __shfl_sync(0xFFFFFFFFu, words, k);
+        // The run of leaf children before the next internal child of the
+        // union: each lane accumulates its own hit leaves of the run in index
+        // order (the warp loops over the largest count), which is the order
+        // of its own traversal.  A lane's mask bits of passed children are
+        // never read again, so they are left set.
+        const uint32_t inner_left = uni & ~leaves;
+        const uint32_t run = inner_left ? uni & ((inner_left & (0u - inner_left)) - 1u) : uni;
+        if (run) {
+            uni &= ~run;
+            uint32_t mine_run = own & run;
+            while (__any_sync(0xFFFFFFFFu, mine_run != 0)) {
+                const bool hit = mine_run != 0;
+                const uint32_t k = hit ? __ffs(mine_run) - 1 : 0u;
+                mine_run &= mine_run - 1;
+                const uint32_t child = __shfl_sync(0xFFFFFFFFu, words, k);
+                float t0, t1;
+                child_span(slabs, k, t0, t1);
+                const V3 color = leaf_rgb(a.color(child));
+                if (COUNT && hit) loads += 2;  // the child's is_leaf_depth and colour
+                // a lane without a leaf here adds color * 0 = +0, which
+                // leaves its sum (never -0) unchanged
+                total = total + color * (hit ? t1 - t0 : 0.0f);
+            }
+            if (uni == 0) continue;
         }
-        if (uni == 0 || a.is_leaf(child)) continue;
+        // the lowest child left is internal: descend into it (lanes that
+        // miss it sit out its subtree)
+        const uint32_t k = __ffs(uni) - 1;
+        const uint32_t child = __shfl_sync(0xFFFFFFFFu, words, k);
         uni &= uni - 1;
         const bool mine = (own >> k) & 1u;
         if (COUNT && mine) ++loads;
-        // descend into child k (lanes that miss it sit out its subtree)
         if (uni != 0) {
             if (sp >= STACK_DEPTH) {
                 if (active) err |= 2u;
@@ -1081,6 +1093,7 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
                     origin.z + ((k & 1u) ? side : 0.0f));
         node = child;
         words = a.child(node, slot);
+        leaves = __ballot_sync(0xFFFFFFFFu, a.is_leaf(words)) & 0xFFu;
         side *= 0.5f;
         slabs = child_slabs(origin, side, rrd, bias);
         own = mine ? hit_mask(slabs) : 0u;
