@@ -276,10 +276,11 @@ struct FindPath {
 // extents of depth <= 24 are exact floats either way.
 
 __device__ __forceinline__ uint32_t fix_coord(float p) {
-    // floor(p * 2^30) (the scaling is exact); the conversion saturates and
-    // the clamp then gives the open bounds of the border cells
-    const int v = __float2int_rd(p * 1073741824.0f);
-    return (uint32_t)min(max(v, 0), (1 << FIX_BITS) - 1);
+    // floor(p * 2^30) (the scaling is exact); the unsigned conversion
+    // saturates (negative values to 0) and the clamp then gives the open
+    // bounds of the border cells
+    const uint32_t v = __float2uint_rd(p * 1073741824.0f);
+    return min(v, (1u << FIX_BITS) - 1u);
 }
 
 __device__ __forceinline__ float fix_to_float(uint32_t v) { return (float)v * (1.0f / 1073741824.0f); }
@@ -767,11 +768,21 @@ __device__ __forceinline__ uint32_t find_relative(const Acc& a, uint32_t parent,
     }
 }
 
-// resources/svo_rope.comp:50-63
-__device__ __forceinline__ uint32_t neighbor_index(uint32_t nx, uint32_t ny, uint32_t nz, V3 far, V3& mask) {
-    if (far.x < fminf(far.y, far.z)) { mask = v3(1.f, 0.f, 0.f); return nx; }
-    if (far.y < far.z) { mask = v3(0.f, 1.f, 0.f); return ny; }
-    mask = v3(0.f, 0.f, 1.f);
+// resources/svo_rope.comp:50-63.  The reference returns a one-hot mask and
+// moves the offset by (mask * sgn) * side: the chosen axis by sgn * side,
+// the others by +-0, which leaves them unchanged (offsets are never -0).  So
+// only the chosen axis is moved here.
+__device__ __forceinline__ uint32_t neighbor_index(uint32_t nx, uint32_t ny, uint32_t nz, V3 far, V3 sgn, float side,
+                                                   V3& offset) {
+    if (far.x < fminf(far.y, far.z)) {
+        offset.x = offset.x + sgn.x * side;
+        return nx;
+    }
+    if (far.y < far.z) {
+        offset.y = offset.y + sgn.y * side;
+        return ny;
+    }
+    offset.z = offset.z + sgn.z * side;
     return nz;
 }
 
@@ -803,11 +814,9 @@ __device__ V3 trace_rope(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& 
     float step = u_max - fmaxf(u_min, 0.0f);
     V3 color = leaf_rgb(a.color(node));
     V3 total = color * step;
-    V3 mask;
-    uint32_t n = neighbor_index(nbx, nby, nbz, far, mask);
+    uint32_t n = neighbor_index(nbx, nby, nbz, far, sgn, side, offset);
     node = a.child(node, n);
     if (COUNT) loads += 2;
-    offset = offset + (mask * sgn) * side;
     uint32_t iter = 0;
     while (node != a.exit_word()) {
         if (++iter > SVO_MAX_ITER) { err |= 1u; break; }
@@ -821,10 +830,9 @@ __device__ V3 trace_rope(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& 
         step = u_max - fmaxf(u_min, 0.0f);
         color = leaf_rgb(a.color(node));
         total = total + color * step;
-        n = neighbor_index(nbx, nby, nbz, far, mask);
+        n = neighbor_index(nbx, nby, nbz, far, sgn, side, offset);
         node = a.child(node, n);
         if (COUNT) loads += 2;
-        offset = offset + (mask * sgn) * side;
     }
     return total;
 }
