@@ -10,6 +10,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -485,6 +486,14 @@ int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_p
         // masked svo-df walked by the whole warp unless XN_DF_PACKET=0
         const char* pk = std::getenv("XN_DF_PACKET");
         L.df_packet = !(pk && pk[0] == '0');
+        // the nodes one level above the deepest internal nodes (children:
+        // leaves and internal nodes whose children are all leaves) are walked
+        // by each lane alone, unless XN_DF_LANE_WALK=0
+        const char* lw = std::getenv("XN_DF_LANE_WALK");
+        const uint32_t dmax = v->max_inner_depth;
+        L.df_lane_side = (lw && lw[0] == '0') || !v->depth_consistent || dmax < 1u || dmax > 120u
+                             ? 0.0f
+                             : std::ldexp(1.0f, -(int)dmax);
     }
     for (int i = 0; i < 3; ++i) L.dim[i] = v->dim[i];
     return XN_OK;

@@ -1009,8 +1009,54 @@ struct PacketStacksColumns {
     __device__ __forceinline__ void set_mask(int i, uint32_t m) { mine[i * stride] = m; }
 };
 
+// A node one level above the deepest internal nodes has only leaves and
+// internal children whose children are all leaves.  There the lanes part:
+// each lane takes its own hit children in index order, accumulates a leaf
+// child, and for an internal child takes that child's hit mask and
+// accumulates its hit leaves in index order -- its own traversal of the node,
+// with the same arithmetic and word reads.  The warp loops over the largest
+// count of hit children instead of their union.  `words` holds the node's
+// child words (lane j: word j & 7).
+template <bool COUNT, class Acc>
+__device__ __forceinline__ void lane_walk(const Acc& a, uint32_t words, uint32_t own, V3 origin, float side,
+                                          const ChildSlabs& slabs, V3 rrd, V3 bias, V3& total, uint32_t& loads) {
+    while (__any_sync(0xFFFFFFFFu, own != 0)) {
+        const bool has = own != 0;
+        const uint32_t k = has ? __ffs(own) - 1 : 0u;
+        own &= own - 1;
+        const uint32_t c = __shfl_sync(0xFFFFFFFFu, words, k);
+        if (a.is_leaf(c)) {
+            float t0, t1;
+            child_span(slabs, k, t0, t1);
+            const V3 color = leaf_rgb(a.color(c));
+            if (COUNT && has) loads += 2;  // the child's is_leaf_depth and colour
+            // a lane without a child here adds color * 0 = +0
+            total = total + color * (has ? t1 - t0 : 0.0f);
+        } else if (has) {
+            // descend into c (its is_leaf_depth and 8 children; the pop back
+            // reads this node's depth unless k == 7), accumulate its hit leaves
+            if (COUNT) loads += 9u + (k != 7u ? 1u : 0u);
+            const V3 co = v3(origin.x + ((k & 4u) ? side : 0.0f), origin.y + ((k & 2u) ? side : 0.0f),
+                             origin.z + ((k & 1u) ? side : 0.0f));
+            const ChildSlabs cs = child_slabs(co, side * 0.5f, rrd, bias);
+            uint32_t m = hit_mask(cs);
+            while (m != 0) {
+                const uint32_t j = __ffs(m) - 1;
+                m &= m - 1;
+                float t0, t1;
+                child_span(cs, j, t0, t1);
+                if (COUNT) loads += 2;
+                total = total + leaf_rgb(a.color(a.child(c, j))) * (t1 - t0);
+            }
+        }
+    }
+}
+
+// lane_side: the child size 2^-D of the nodes the lanes walk alone (D: the
+// deepest internal node's depth), or 0.
 template <bool COUNT, class Acc, class PS>
-__device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t& loads, uint32_t& err, PS& ps) {
+__device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t& loads, uint32_t& err, PS& ps,
+                              float lane_side = 0.0f) {
     const V3 rrd = vs(1.0f) / rd;
     const V3 bias = rrd * ro;
     int sp = 0;
@@ -1027,7 +1073,13 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
     ChildSlabs slabs = child_slabs(origin, side, rrd, bias);
     uint32_t own = active ? hit_mask(slabs) : 0u;
     if (COUNT && active) loads += 8;
-    uint32_t uni = __reduce_or_sync(0xFFFFFFFFu, own);
+    uint32_t uni;
+    if (side == lane_side) {
+        lane_walk<COUNT>(a, words, own, origin, side, slabs, rrd, bias, total, loads);
+        uni = 0;
+    } else {
+        uni = __reduce_or_sync(0xFFFFFFFFu, own);
+    }
     // Between two pops the walk only descends, and after about 150 descents
     // the child size is 0 and no child is hit; so a cap on the pops bounds
     // the loop.
@@ -1101,18 +1153,23 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
                     origin.z + ((k & 1u) ? side : 0.0f));
         node = child;
         words = a.child(node, slot);
-        leaves = __ballot_sync(0xFFFFFFFFu, a.is_leaf(words)) & 0xFFu;
         side *= 0.5f;
         slabs = child_slabs(origin, side, rrd, bias);
         own = mine ? hit_mask(slabs) : 0u;
         if (COUNT && mine) loads += 8;
-        uni = __reduce_or_sync(0xFFFFFFFFu, own);
+        if (side == lane_side) {
+            lane_walk<COUNT>(a, words, own, origin, side, slabs, rrd, bias, total, loads);
+            uni = 0;
+        } else {
+            leaves = __ballot_sync(0xFFFFFFFFu, a.is_leaf(words)) & 0xFFu;
+            uni = __reduce_or_sync(0xFFFFFFFFu, own);
+        }
     }
     return total;
 }
 
 template <bool COUNT, class Acc>
-__global__ void __launch_bounds__(BLOCK_THREADS) df_packet_kernel(Frame f, Acc a, Outputs o) {
+__global__ void __launch_bounds__(BLOCK_THREADS) df_packet_kernel(Frame f, Acc a, Outputs o, float lane_side) {
     __shared__ float4 s_geo[(BLOCK_THREADS / 32) * STACK_DEPTH];
     __shared__ uint2 s_ns[(BLOCK_THREADS / 32) * STACK_DEPTH];
     __shared__ uint8_t s_mask[(BLOCK_THREADS / 32) * STACK_DEPTH * 32];
@@ -1124,7 +1181,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) df_packet_kernel(Frame f, Acc a
     uint32_t loads = 0, err = 0;
     PacketStacksWarp ps{s_ns + warp * STACK_DEPTH, s_geo + warp * STACK_DEPTH, s_mask + warp * STACK_DEPTH * 32,
                         threadIdx.x & 31u};
-    const V3 total = trace_df_packet<COUNT>(a, f.translation, rd, active, loads, err, ps);
+    const V3 total = trace_df_packet<COUNT>(a, f.translation, rd, active, loads, err, ps, lane_side);
     if (active) write_outputs(f, o, ix, iy, total * voxel_emission_coeff(f, rd), loads, err);
 }
 
@@ -1224,8 +1281,8 @@ cudaError_t launch_render(const RenderLaunch& L, cudaStream_t stream) {
         }
     } else if (L.traversal == XN_TRAV_SVO_DF && L.df_packet && L.layout == XN_LAYOUT_COMPACT && L.depth_consistent) {
         const CompactNodes acc{L.inner, L.inner_depth};
-        if (count) df_packet_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
-        else df_packet_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o);
+        if (count) df_packet_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o, L.df_lane_side);
+        else df_packet_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o, L.df_lane_side);
     } else if (L.traversal == XN_TRAV_SVO_DF && L.shared_stacks && L.layout == XN_LAYOUT_COMPACT &&
                L.depth_consistent) {
         const CompactNodes acc{L.inner, L.inner_depth};

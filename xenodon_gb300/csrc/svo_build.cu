@@ -1225,6 +1225,11 @@ XN_API int xn_build_svo_volume(xn_ctx* h, const void* d_rgba, uint32_t dx, uint3
             v->dim[0] = v->dim[1] = v->dim[2] = (uint32_t)sd;
             v->layout = XN_LAYOUT_COMPACT;
             v->depth_consistent = 1;  // written from the tree itself
+            if ((r = measure_inner_depth(c, v))) {
+                v->release_layout();
+                delete v;
+                return r;
+            }
             *out = reinterpret_cast<xn_volume*>(v);
             return XN_OK;
         }

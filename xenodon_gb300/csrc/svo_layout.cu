@@ -110,7 +110,36 @@ __global__ void depth_check_kernel(const uint32_t* w, uint64_t n, uint32_t* bad)
     if (local) atomicOr(bad, 1u);
 }
 
+// The largest depth field of the internal nodes.
+__global__ void max_inner_depth_kernel(const uint32_t* depth, uint64_t n, uint32_t* out) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    uint32_t m = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        m = max(m, depth[i] & 0x7FFFFFFFu);
+    m = __reduce_max_sync(0xFFFFFFFFu, m);
+    if ((threadIdx.x & 31u) == 0) atomicMax(out, m);
+}
+
 }  // namespace
+
+int measure_inner_depth(Ctx* c, Volume* v) {
+    v->max_inner_depth = 0xFFFFFFFFu;
+    if (!v->depth_consistent || !v->inner_depth || v->n_inner == 0) return XN_OK;
+    uint32_t* d = nullptr;
+    uint32_t h = 0xFFFFFFFFu;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&d), 4, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, 4, c->stream);
+    if (e == cudaSuccess) {
+        max_inner_depth_kernel<<<1024, 256, 0, c->stream>>>(v->inner_depth, v->n_inner, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, 4, cudaMemcpyDeviceToHost, c->stream);
+    if (d) cudaFreeAsync(d, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "octree depth");
+    v->max_inner_depth = h;
+    return XN_OK;
+}
 
 int build_svo_layout(Ctx* c, Volume* v) {
     const uint64_t n = v->n_nodes;
@@ -208,6 +237,10 @@ int build_svo_layout(Ctx* c, Volume* v) {
         return r;
     }
     v->layout = XN_LAYOUT_COMPACT;
+    if ((r = measure_inner_depth(c, v))) {
+        v->release_layout();
+        return r;
+    }
     // the reference nodes are no longer needed on the device
     c->device_free(v->data, v->bytes);
     v->data = nullptr;

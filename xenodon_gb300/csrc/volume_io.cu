@@ -314,6 +314,7 @@ XN_API int xn_volume_load(xn_ctx* h, const char* path, xn_volume** out) {
     if (hf[0]) return drop(fail(XN_ERR_FORMAT, "'%s': an index is out of range", path));
     v->depth_consistent = hf[1] == 0;
     v->layout = XN_LAYOUT_COMPACT;
+    if ((r = measure_inner_depth(c, v))) return drop(r);
     *out = reinterpret_cast<xn_volume*>(v);
     return XN_OK;
 }

@@ -67,6 +67,7 @@ struct Volume {
     uint32_t* inner_depth = nullptr;
     uint32_t* leaves = nullptr;
     int depth_consistent = 0;  // internal nodes' depth fields match the tree (svo_layout.cu)
+    uint32_t max_inner_depth = 0xFFFFFFFFu;  // deepest internal node of a depth-consistent tree, else ~0
 
     uint64_t layout_bytes() const {
         return (inner ? n_inner * 32 : 0) + (rinner ? n_inner * 32 : 0) + (inner_depth ? n_inner * 4 : 0) +
@@ -83,6 +84,9 @@ struct Volume {
 };
 
 int build_svo_layout(Ctx* c, Volume* v);
+// Sets v->max_inner_depth from the internal nodes' depth fields when the tree
+// is depth-consistent (svo_layout.cu).
+int measure_inner_depth(Ctx* c, Volume* v);
 
 // Octree build on the device (svo_build.cu).  With lean == nullptr: the
 // reference node array in *d_nodes.  With lean: only the device layout's
