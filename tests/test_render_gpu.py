@@ -337,9 +337,10 @@ def test_df_walked_by_the_warp_equals_one_ray_per_thread(ctx, blob_volumes, monk
 @pytest.mark.parametrize("n", [2, 4, 16, 64])
 @pytest.mark.parametrize("cam", ["oblique", "inside", "grazing"])
 def test_df_lane_walk_equals_warp_walk(ctx, monkeypatch, n, cam):
-    # the nodes one level above the deepest internal nodes are walked by each
-    # lane alone; XN_DF_LANE_WALK=0 keeps the warp walk there: same bits,
-    # same word counts, on trees 1 to 6 levels deep
+    # the nodes just above the deepest internal nodes are walked by each lane
+    # alone, two levels deep (one with XN_DF_LANE_LEVELS=1); XN_DF_LANE_WALK=0
+    # keeps the warp walk there: same bits, same word counts, on trees 1 to 6
+    # levels deep
     import xenodon_gb300 as xg
     from xenodon_gb300 import volumes
     g = volumes.random_grid(n, n, n, seed=n + 1, density=0.35, levels=4)
@@ -348,11 +349,16 @@ def test_df_lane_walk_equals_warp_walk(ctx, monkeypatch, n, cam):
     p, v = _params_pair(xg, 61, 45)
     lane, _ = check_parity(ctx, "svo-df", CAMS[cam], p, v, nodes=nodes, vol=vol, label=f"df-lane/{n}/{cam}")
     _, em_l, loads_l = _gpu_counts(ctx, vol, "svo-df", xg.make_camera(*CAMS[cam]), p)
+    monkeypatch.setenv("XN_DF_LANE_LEVELS", "1")
+    one, _, _ = ctx.render(vol, "svo-df", xg.make_camera(*CAMS[cam]), p)
+    _, em_1, loads_1 = _gpu_counts(ctx, vol, "svo-df", xg.make_camera(*CAMS[cam]), p)
+    monkeypatch.delenv("XN_DF_LANE_LEVELS")
     monkeypatch.setenv("XN_DF_LANE_WALK", "0")
     warp, _, _ = ctx.render(vol, "svo-df", xg.make_camera(*CAMS[cam]), p)
     _, em_w, loads_w = _gpu_counts(ctx, vol, "svo-df", xg.make_camera(*CAMS[cam]), p)
-    assert np.array_equal(lane, warp)
+    assert np.array_equal(lane, warp) and np.array_equal(one, warp)
     assert np.array_equal(em_l, em_w) and np.array_equal(loads_l, loads_w)
+    assert np.array_equal(em_1, em_w) and np.array_equal(loads_1, loads_w)
 
 
 @pytest.mark.parametrize("cam", ["front", "inside", "grazing"])

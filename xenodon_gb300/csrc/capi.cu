@@ -486,14 +486,17 @@ int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_p
         // masked svo-df walked by the whole warp unless XN_DF_PACKET=0
         const char* pk = std::getenv("XN_DF_PACKET");
         L.df_packet = !(pk && pk[0] == '0');
-        // the nodes one level above the deepest internal nodes (children:
-        // leaves and internal nodes whose children are all leaves) are walked
-        // by each lane alone, unless XN_DF_LANE_WALK=0
+        // the nodes just above the deepest internal nodes are walked by each
+        // lane alone (render.cu, lane_walk), unless XN_DF_LANE_WALK=0
         const char* lw = std::getenv("XN_DF_LANE_WALK");
         const uint32_t dmax = v->max_inner_depth;
+        // two levels (from the nodes two above the deepest internal ones)
+        // unless the tree is shallower or XN_DF_LANE_LEVELS=1
+        const char* ll = std::getenv("XN_DF_LANE_LEVELS");
+        L.df_lane_levels = (ll && ll[0] == '1') || dmax < 2u ? 1 : 2;
         L.df_lane_side = (lw && lw[0] == '0') || !v->depth_consistent || dmax < 1u || dmax > 120u
                              ? 0.0f
-                             : std::ldexp(1.0f, -(int)dmax);
+                             : std::ldexp(1.0f, -(int)dmax + (L.df_lane_levels - 1));
     }
     for (int i = 0; i < 3; ++i) L.dim[i] = v->dim[i];
     return XN_OK;

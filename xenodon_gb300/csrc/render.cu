@@ -1052,9 +1052,68 @@ __device__ __forceinline__ void lane_walk(const Acc& a, uint32_t words, uint32_t
     }
 }
 
-// lane_side: the child size 2^-D of the nodes the lanes walk alone (D: the
-// deepest internal node's depth), or 0.
-template <bool COUNT, class Acc, class PS>
+// The same walk for a node that only this lane visits (its own child words
+// are loaded per lane): node c with origin co, child size cs and hit mask m.
+template <bool COUNT, class Acc>
+__device__ __forceinline__ void lane_walk_own(const Acc& a, uint32_t c, V3 co, float cs, uint32_t m,
+                                              const ChildSlabs& csl, V3 rrd, V3 bias, V3& total, uint32_t& loads) {
+    while (m != 0) {
+        const uint32_t k = __ffs(m) - 1;
+        m &= m - 1;
+        const uint32_t w = a.child(c, k);
+        if (a.is_leaf(w)) {
+            float t0, t1;
+            child_span(csl, k, t0, t1);
+            if (COUNT) loads += 2;
+            total = total + leaf_rgb(a.color(w)) * (t1 - t0);
+        } else {
+            if (COUNT) loads += 9u + (k != 7u ? 1u : 0u);
+            const V3 o2 = v3(co.x + ((k & 4u) ? cs : 0.0f), co.y + ((k & 2u) ? cs : 0.0f),
+                             co.z + ((k & 1u) ? cs : 0.0f));
+            const ChildSlabs s2 = child_slabs(o2, cs * 0.5f, rrd, bias);
+            uint32_t m2 = hit_mask(s2);
+            while (m2 != 0) {
+                const uint32_t j = __ffs(m2) - 1;
+                m2 &= m2 - 1;
+                float t0, t1;
+                child_span(s2, j, t0, t1);
+                if (COUNT) loads += 2;
+                total = total + leaf_rgb(a.color(a.child(w, j))) * (t1 - t0);
+            }
+        }
+    }
+}
+
+// Two levels above the deepest internal nodes: each lane walks its own hit
+// children, and below them everything, alone.
+template <bool COUNT, class Acc>
+__device__ __forceinline__ void lane_walk2(const Acc& a, uint32_t words, uint32_t own, V3 origin, float side,
+                                           const ChildSlabs& slabs, V3 rrd, V3 bias, V3& total, uint32_t& loads) {
+    while (__any_sync(0xFFFFFFFFu, own != 0)) {
+        const bool has = own != 0;
+        const uint32_t k = has ? __ffs(own) - 1 : 0u;
+        own &= own - 1;
+        const uint32_t c = __shfl_sync(0xFFFFFFFFu, words, k);
+        if (a.is_leaf(c)) {
+            float t0, t1;
+            child_span(slabs, k, t0, t1);
+            const V3 color = leaf_rgb(a.color(c));
+            if (COUNT && has) loads += 2;
+            total = total + color * (has ? t1 - t0 : 0.0f);
+        } else if (has) {
+            if (COUNT) loads += 9u + (k != 7u ? 1u : 0u);
+            const V3 co = v3(origin.x + ((k & 4u) ? side : 0.0f), origin.y + ((k & 2u) ? side : 0.0f),
+                             origin.z + ((k & 1u) ? side : 0.0f));
+            const float cs = side * 0.5f;
+            const ChildSlabs csl = child_slabs(co, cs, rrd, bias);
+            lane_walk_own<COUNT>(a, c, co, cs, hit_mask(csl), csl, rrd, bias, total, loads);
+        }
+    }
+}
+
+// lane_side: the child size of the nodes the lanes walk alone (LEVELS = 1:
+// 2^-D, D the deepest internal node's depth; LEVELS = 2: 2^-(D-1)), or 0.
+template <bool COUNT, class Acc, class PS, int LEVELS = 1>
 __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t& loads, uint32_t& err, PS& ps,
                               float lane_side = 0.0f) {
     const V3 rrd = vs(1.0f) / rd;
@@ -1075,7 +1134,8 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
     if (COUNT && active) loads += 8;
     uint32_t uni;
     if (side == lane_side) {
-        lane_walk<COUNT>(a, words, own, origin, side, slabs, rrd, bias, total, loads);
+        if (LEVELS == 2) lane_walk2<COUNT>(a, words, own, origin, side, slabs, rrd, bias, total, loads);
+            else lane_walk<COUNT>(a, words, own, origin, side, slabs, rrd, bias, total, loads);
         uni = 0;
     } else {
         uni = __reduce_or_sync(0xFFFFFFFFu, own);
@@ -1158,7 +1218,8 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
         own = mine ? hit_mask(slabs) : 0u;
         if (COUNT && mine) loads += 8;
         if (side == lane_side) {
-            lane_walk<COUNT>(a, words, own, origin, side, slabs, rrd, bias, total, loads);
+            if (LEVELS == 2) lane_walk2<COUNT>(a, words, own, origin, side, slabs, rrd, bias, total, loads);
+            else lane_walk<COUNT>(a, words, own, origin, side, slabs, rrd, bias, total, loads);
             uni = 0;
         } else {
             leaves = __ballot_sync(0xFFFFFFFFu, a.is_leaf(words)) & 0xFFu;
@@ -1168,7 +1229,7 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
     return total;
 }
 
-template <bool COUNT, class Acc>
+template <bool COUNT, class Acc, int LEVELS = 1>
 __global__ void __launch_bounds__(BLOCK_THREADS) df_packet_kernel(Frame f, Acc a, Outputs o, float lane_side) {
     __shared__ float4 s_geo[(BLOCK_THREADS / 32) * STACK_DEPTH];
     __shared__ uint2 s_ns[(BLOCK_THREADS / 32) * STACK_DEPTH];
@@ -1181,7 +1242,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS) df_packet_kernel(Frame f, Acc a
     uint32_t loads = 0, err = 0;
     PacketStacksWarp ps{s_ns + warp * STACK_DEPTH, s_geo + warp * STACK_DEPTH, s_mask + warp * STACK_DEPTH * 32,
                         threadIdx.x & 31u};
-    const V3 total = trace_df_packet<COUNT>(a, f.translation, rd, active, loads, err, ps, lane_side);
+    const V3 total = trace_df_packet<COUNT, Acc, PacketStacksWarp, LEVELS>(a, f.translation, rd, active, loads, err,
+                                                                          ps, lane_side);
     if (active) write_outputs(f, o, ix, iy, total * voxel_emission_coeff(f, rd), loads, err);
 }
 
@@ -1281,8 +1343,13 @@ cudaError_t launch_render(const RenderLaunch& L, cudaStream_t stream) {
         }
     } else if (L.traversal == XN_TRAV_SVO_DF && L.df_packet && L.layout == XN_LAYOUT_COMPACT && L.depth_consistent) {
         const CompactNodes acc{L.inner, L.inner_depth};
-        if (count) df_packet_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o, L.df_lane_side);
-        else df_packet_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o, L.df_lane_side);
+        if (L.df_lane_levels == 2) {
+            if (count) df_packet_kernel<true, CompactNodes, 2><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o, L.df_lane_side);
+            else df_packet_kernel<false, CompactNodes, 2><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o, L.df_lane_side);
+        } else {
+            if (count) df_packet_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o, L.df_lane_side);
+            else df_packet_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, acc, o, L.df_lane_side);
+        }
     } else if (L.traversal == XN_TRAV_SVO_DF && L.shared_stacks && L.layout == XN_LAYOUT_COMPACT &&
                L.depth_consistent) {
         const CompactNodes acc{L.inner, L.inner_depth};

@@ -49,8 +49,10 @@ struct RenderLaunch {
     int shared_stacks;            // esvo and masked svo-df with their stacks in shared memory
     int naive_resume;             // svo-naive's find resumes from the previous step's path
     int df_packet;                // masked svo-df walked by the whole warp (df_packet_kernel)
-    float df_lane_side;           // child size 2^-D of the nodes whose children the lanes walk alone
-                                  // (D: the deepest internal node's depth), or 0
+    float df_lane_side;           // child size of the nodes below which the lanes walk alone: 2^-D
+                                  // (one level; D the deepest internal node's depth) or 2^-(D-1)
+                                  // (two levels), or 0
+    int df_lane_levels;           // 1 or 2
     // outputs (device pointers)
     void* d_rgba;
     float* d_emission;
