@@ -667,38 +667,40 @@ __device__ V3 trace_esvo(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& 
         idx = cxor(idx, ax, ay, az);
     }
     V3 total = vs(0.0f);
-    uint32_t iter = 0;
+    // Between two pops the loop descends at most `depth` times (the scale
+    // runs out) and advances at most 3 times per level, so a cap on the pops
+    // bounds it.
+    uint32_t pops = 0;
     while (scale < depth) {
-        if (++iter > SVO_MAX_ITER) { err |= 1u; break; }
         V3 t_corner = pos * t_coeff - t_bias;
         float tc_max = min_elem(t_corner);
-        if (t_min <= t_max) {
-            float tv_max = fminf(t_max, tc_max);
-            if (t_min <= tv_max) {
-                uint32_t child = a.child(parent, idx ^ octant_mask);
-                if (COUNT) loads += 2;
-                if (a.is_leaf(child)) {
-                    V3 color = leaf_rgb(a.color(child));
-                    if (COUNT) ++loads;
-                    total = total + color * (tv_max - t_min);
-                } else {
-                    if (tc_max < h) {
-                        stk.first(scale) = parent;
-                        stk.second(scale) = __float_as_uint(t_max);
-                    }
-                    h = tc_max;
-                    parent = child;
-                    --scale;
-                    scale_exp2 *= 0.5f;
-                    V3 t_center = t_coeff * scale_exp2 + t_corner;
-                    bool ax = t_center.x > t_min, ay = t_center.y > t_min, az = t_center.z > t_min;
-                    idx = cxor(0u, ax, ay, az);
-                    if (ax) pos.x = pos.x + scale_exp2;
-                    if (ay) pos.y = pos.y + scale_exp2;
-                    if (az) pos.z = pos.z + scale_exp2;
-                    t_max = tv_max;
-                    continue;
+        // the reference tests t_min <= t_max and then t_min <= tv_max; as
+        // tv_max <= t_max, the second test alone decides
+        float tv_max = fminf(t_max, tc_max);
+        if (t_min <= tv_max) {
+            uint32_t child = a.child(parent, idx ^ octant_mask);
+            if (COUNT) loads += 2;
+            if (a.is_leaf(child)) {
+                V3 color = leaf_rgb(a.color(child));
+                if (COUNT) ++loads;
+                total = total + color * (tv_max - t_min);
+            } else {
+                if (tc_max < h) {
+                    stk.first(scale) = parent;
+                    stk.second(scale) = __float_as_uint(t_max);
                 }
+                h = tc_max;
+                parent = child;
+                --scale;
+                scale_exp2 *= 0.5f;
+                V3 t_center = t_coeff * scale_exp2 + t_corner;
+                bool ax = t_center.x > t_min, ay = t_center.y > t_min, az = t_center.z > t_min;
+                idx = cxor(0u, ax, ay, az);
+                if (ax) pos.x = pos.x + scale_exp2;
+                if (ay) pos.y = pos.y + scale_exp2;
+                if (az) pos.z = pos.z + scale_exp2;
+                t_max = tv_max;
+                continue;
             }
         }
         // ADVANCE
@@ -711,6 +713,7 @@ __device__ V3 trace_esvo(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& 
         idx ^= step_mask;
         if ((idx & step_mask) != 0) {
             // POP
+            if (++pops > SVO_MAX_ITER) { err |= 1u; break; }
             uint32_t xx = __float_as_uint(pos.x) ^ __float_as_uint(pos.x + scale_exp2);
             uint32_t xy = __float_as_uint(pos.y) ^ __float_as_uint(pos.y + scale_exp2);
             uint32_t xz = __float_as_uint(pos.z) ^ __float_as_uint(pos.z + scale_exp2);
