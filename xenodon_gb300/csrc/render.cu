@@ -1414,6 +1414,9 @@ BatchJob make_batch_job(const RenderLaunch& L) {
     j.leaves = L.leaves;
     j.rgba = L.d_rgba;
     j.depth_consistent = L.depth_consistent;
+    // the batch's svo-df form walks one level per lane (its blocks of up to
+    // 1024 threads leave 64 registers a thread): child size 2^-D
+    j.df_lane_side = L.df_lane_levels == 2 ? L.df_lane_side * 0.5f : L.df_lane_side;
     return j;
 }
 
@@ -1533,7 +1536,7 @@ __device__ __forceinline__ uint32_t render_job_pixel_spec(const BatchJob& J, uin
         PacketStacksColumns ps{stk->a - lane, stk->b, stk->stride};
         uint32_t loads = 0;
         const V3 total = trace_df_packet<false>(CompactNodes{J.inner, J.inner_depth}, f.translation, rd, active,
-                                                loads, err, ps);
+                                                loads, err, ps, J.df_lane_side);
         return pack_rgba(total * voxel_emission_coeff(f, rd));
     }
     if constexpr (SPEC == XN_BATCH_ANY) {

@@ -76,6 +76,7 @@ struct alignas(16) BatchJob {
     int32_t tex_normalized;
     int32_t depth_consistent;
     int32_t form;  // XN_BATCH_* form of this job (batch_spec)
+    float df_lane_side;  // svo-df: child size 2^-D of the nodes whose children the lanes walk alone, or 0
     unsigned long long tex;
     const void* grid;
     const void* nodes;
