@@ -1012,15 +1012,64 @@ struct PacketStacksColumns {
     __device__ __forceinline__ void set_mask(int i, uint32_t m) { mine[i * stride] = m; }
 };
 
-// A node one level above the deepest internal nodes has only leaves and
-// internal children whose children are all leaves.  There the lanes part:
-// each lane takes its own hit children in index order, accumulates a leaf
-// child, and for an internal child takes that child's hit mask and
-// accumulates its hit leaves in index order -- its own traversal of the node,
-// with the same arithmetic and word reads.  The warp loops over the largest
-// count of hit children instead of their union.  `words` holds the node's
-// child words (lane j: word j & 7).
+// The bottom of the octree walked by each lane alone.  In a depth-consistent
+// tree whose deepest internal nodes are at depth D, a node at depth D-1 has
+// only leaves and internal children whose children are all leaves, and a
+// node at depth D-2 only leaves and such D-1 nodes.  Below such a node each
+// lane takes its own hit children in index order: a leaf is accumulated, an
+// internal child gets its own hit mask and is walked the same way.  That is
+// the lane's own traversal, with the same arithmetic and word reads; the warp
+// loops over the largest per-lane count instead of the union.
+
+// The hit leaves of node c (origin co, child size cs; all children leaves),
+// in index order.
 template <bool COUNT, class Acc>
+__device__ __forceinline__ void lane_leaves(const Acc& a, uint32_t c, V3 co, float cs, V3 rrd, V3 bias, V3& total,
+                                            uint32_t& loads) {
+    const ChildSlabs sl = child_slabs(co, cs, rrd, bias);
+    uint32_t m = hit_mask(sl);
+    while (m != 0) {
+        const uint32_t j = __ffs(m) - 1;
+        m &= m - 1;
+        float t0, t1;
+        child_span(sl, j, t0, t1);
+        if (COUNT) loads += 2;  // the leaf's is_leaf_depth and colour
+        total = total + leaf_rgb(a.color(a.child(c, j))) * (t1 - t0);
+    }
+}
+
+// Origin of child k of a node with origin o and child size s.
+__device__ __forceinline__ V3 child_origin(V3 o, float s, uint32_t k) {
+    return v3(o.x + ((k & 4u) ? s : 0.0f), o.y + ((k & 2u) ? s : 0.0f), o.z + ((k & 1u) ? s : 0.0f));
+}
+
+// Node c at depth D-1 (origin co, child size cs), visited by this lane only.
+template <bool COUNT, class Acc>
+__device__ __forceinline__ void lane_walk_own(const Acc& a, uint32_t c, V3 co, float cs, V3 rrd, V3 bias, V3& total,
+                                              uint32_t& loads) {
+    const ChildSlabs sl = child_slabs(co, cs, rrd, bias);
+    uint32_t m = hit_mask(sl);
+    while (m != 0) {
+        const uint32_t k = __ffs(m) - 1;
+        m &= m - 1;
+        const uint32_t w = a.child(c, k);
+        if (a.is_leaf(w)) {
+            float t0, t1;
+            child_span(sl, k, t0, t1);
+            if (COUNT) loads += 2;
+            total = total + leaf_rgb(a.color(w)) * (t1 - t0);
+        } else {
+            // descend (its is_leaf_depth and 8 children; the pop back reads
+            // this node's depth unless k == 7)
+            if (COUNT) loads += 9u + (k != 7u ? 1u : 0u);
+            lane_leaves<COUNT>(a, w, child_origin(co, cs, k), cs * 0.5f, rrd, bias, total, loads);
+        }
+    }
+}
+
+// A node the whole warp holds, LEVELS above the deepest internal nodes:
+// `words` its child words (lane j: word j & 7), `own` this lane's hit mask.
+template <bool COUNT, int LEVELS, class Acc>
 __device__ __forceinline__ void lane_walk(const Acc& a, uint32_t words, uint32_t own, V3 origin, float side,
                                           const ChildSlabs& slabs, V3 rrd, V3 bias, V3& total, uint32_t& loads) {
     while (__any_sync(0xFFFFFFFFu, own != 0)) {
@@ -1032,84 +1081,14 @@ __device__ __forceinline__ void lane_walk(const Acc& a, uint32_t words, uint32_t
             float t0, t1;
             child_span(slabs, k, t0, t1);
             const V3 color = leaf_rgb(a.color(c));
-            if (COUNT && has) loads += 2;  // the child's is_leaf_depth and colour
+            if (COUNT && has) loads += 2;
             // a lane without a child here adds color * 0 = +0
             total = total + color * (has ? t1 - t0 : 0.0f);
         } else if (has) {
-            // descend into c (its is_leaf_depth and 8 children; the pop back
-            // reads this node's depth unless k == 7), accumulate its hit leaves
             if (COUNT) loads += 9u + (k != 7u ? 1u : 0u);
-            const V3 co = v3(origin.x + ((k & 4u) ? side : 0.0f), origin.y + ((k & 2u) ? side : 0.0f),
-                             origin.z + ((k & 1u) ? side : 0.0f));
-            const ChildSlabs cs = child_slabs(co, side * 0.5f, rrd, bias);
-            uint32_t m = hit_mask(cs);
-            while (m != 0) {
-                const uint32_t j = __ffs(m) - 1;
-                m &= m - 1;
-                float t0, t1;
-                child_span(cs, j, t0, t1);
-                if (COUNT) loads += 2;
-                total = total + leaf_rgb(a.color(a.child(c, j))) * (t1 - t0);
-            }
-        }
-    }
-}
-
-// The same walk for a node that only this lane visits (its own child words
-// are loaded per lane): node c with origin co, child size cs and hit mask m.
-template <bool COUNT, class Acc>
-__device__ __forceinline__ void lane_walk_own(const Acc& a, uint32_t c, V3 co, float cs, uint32_t m,
-                                              const ChildSlabs& csl, V3 rrd, V3 bias, V3& total, uint32_t& loads) {
-    while (m != 0) {
-        const uint32_t k = __ffs(m) - 1;
-        m &= m - 1;
-        const uint32_t w = a.child(c, k);
-        if (a.is_leaf(w)) {
-            float t0, t1;
-            child_span(csl, k, t0, t1);
-            if (COUNT) loads += 2;
-            total = total + leaf_rgb(a.color(w)) * (t1 - t0);
-        } else {
-            if (COUNT) loads += 9u + (k != 7u ? 1u : 0u);
-            const V3 o2 = v3(co.x + ((k & 4u) ? cs : 0.0f), co.y + ((k & 2u) ? cs : 0.0f),
-                             co.z + ((k & 1u) ? cs : 0.0f));
-            const ChildSlabs s2 = child_slabs(o2, cs * 0.5f, rrd, bias);
-            uint32_t m2 = hit_mask(s2);
-            while (m2 != 0) {
-                const uint32_t j = __ffs(m2) - 1;
-                m2 &= m2 - 1;
-                float t0, t1;
-                child_span(s2, j, t0, t1);
-                if (COUNT) loads += 2;
-                total = total + leaf_rgb(a.color(a.child(w, j))) * (t1 - t0);
-            }
-        }
-    }
-}
-
-// Two levels above the deepest internal nodes: each lane walks its own hit
-// children, and below them everything, alone.
-template <bool COUNT, class Acc>
-__device__ __forceinline__ void lane_walk2(const Acc& a, uint32_t words, uint32_t own, V3 origin, float side,
-                                           const ChildSlabs& slabs, V3 rrd, V3 bias, V3& total, uint32_t& loads) {
-    while (__any_sync(0xFFFFFFFFu, own != 0)) {
-        const bool has = own != 0;
-        const uint32_t k = has ? __ffs(own) - 1 : 0u;
-        own &= own - 1;
-        const uint32_t c = __shfl_sync(0xFFFFFFFFu, words, k);
-        if (a.is_leaf(c)) {
-            float t0, t1;
-            child_span(slabs, k, t0, t1);
-            const V3 color = leaf_rgb(a.color(c));
-            if (COUNT && has) loads += 2;
-            total = total + color * (has ? t1 - t0 : 0.0f);
-        } else if (has) {
-            if (COUNT) loads += 9u + (k != 7u ? 1u : 0u);
-            const V3 co = v3(origin.x + ((k & 4u) ? side : 0.0f), origin.y + ((k & 2u) ? side : 0.0f),
-                             origin.z + ((k & 1u) ? side : 0.0f));
-            const float cs = side * 0.5f;
-            const ChildSlabs csl = child_slabs(co, cs, rrd, bias);
-            lane_walk_own<COUNT>(a, c, co, cs, hit_mask(csl), csl, rrd, bias, total, loads);
+            const V3 co = child_origin(origin, side, k);
+            if constexpr (LEVELS == 2) lane_walk_own<COUNT>(a, c, co, side * 0.5f, rrd, bias, total, loads);
+            else lane_leaves<COUNT>(a, c, co, side * 0.5f, rrd, bias, total, loads);
         }
     }
 }
@@ -1137,8 +1116,7 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
     if (COUNT && active) loads += 8;
     uint32_t uni;
     if (side == lane_side) {
-        if (LEVELS == 2) lane_walk2<COUNT>(a, words, own, origin, side, slabs, rrd, bias, total, loads);
-            else lane_walk<COUNT>(a, words, own, origin, side, slabs, rrd, bias, total, loads);
+        lane_walk<COUNT, LEVELS>(a, words, own, origin, side, slabs, rrd, bias, total, loads);
         uni = 0;
     } else {
         uni = __reduce_or_sync(0xFFFFFFFFu, own);
@@ -1221,8 +1199,7 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
         own = mine ? hit_mask(slabs) : 0u;
         if (COUNT && mine) loads += 8;
         if (side == lane_side) {
-            if (LEVELS == 2) lane_walk2<COUNT>(a, words, own, origin, side, slabs, rrd, bias, total, loads);
-            else lane_walk<COUNT>(a, words, own, origin, side, slabs, rrd, bias, total, loads);
+            lane_walk<COUNT, LEVELS>(a, words, own, origin, side, slabs, rrd, bias, total, loads);
             uni = 0;
         } else {
             leaves = __ballot_sync(0xFFFFFFFFu, a.is_leaf(words)) & 0xFFu;
