@@ -155,26 +155,51 @@ def make_scene(device: int):
     return grid, path, gen_s
 
 
-def cpu_sample(oracle, grid, nodes, path, frames, row_step, threads):
-    """FP32 oracle over every `row_step`-th row of the given frames; returns
-    (rays, seconds, per-traversal Mrays/s)."""
+def band_offsets(bands: int, rows: int) -> list[int]:
+    """Top rows of `bands` bands of `rows` rows spread evenly over the frame."""
+    bands = max(1, min(bands, HEIGHT // rows))
+    return [((2 * i + 1) * HEIGHT // (2 * bands) - rows // 2) for i in range(bands)]
+
+
+def cpu_sample(oracle, grid, nodes, path, frames, bands, rows, threads):
+    """FP32 oracle over `bands` bands of `rows` full-width rows per frame and
+    traversal, one oracle call (one pool of `threads` threads) per band, so
+    the per-call set-up is small next to the band's work.  Returns (rays,
+    seconds, per-traversal Mrays/s)."""
     rays, secs = 0, 0.0
     per = {t: [0, 0.0] for t in TRAVERSALS}
     for fi in frames:
         f, u, p = path[fi]
         cam = oracle.make_camera(f, u, p)
         for t in TRAVERSALS:
-            for y in range(row_step // 2, HEIGHT, row_step):
-                view = oracle.make_view(WIDTH, HEIGHT, EMISSION, output_offset=(0, y), output_extent=(WIDTH, 1))
+            for y in band_offsets(bands, rows):
+                view = oracle.make_view(WIDTH, HEIGHT, EMISSION, output_offset=(0, y), output_extent=(WIDTH, rows))
                 t0 = time.perf_counter()
                 oracle.render(t, grid=grid if t == "dda" else None, nodes=None if t == "dda" else nodes, camera=cam,
                               view=view, threads=threads, want_loads=False)
                 dt = time.perf_counter() - t0
-                rays += WIDTH
+                rays += WIDTH * rows
                 secs += dt
-                per[t][0] += WIDTH
+                per[t][0] += WIDTH * rows
                 per[t][1] += dt
     return rays, secs, {t: (v[0] / v[1] / 1e6 if v[1] else None) for t, v in per.items()}
+
+
+def cpu_baseline_line(oracle, grid, nodes, path, frames, bands, rows, single_rows):
+    """All host cores on `bands` bands of `rows` rows per frame, and one core
+    on one band of `single_rows` rows of the first frame, per traversal."""
+    threads = os.cpu_count() or 1
+    rays, secs, per = cpu_sample(oracle, grid, nodes, path, frames, bands, rows, threads)
+    r1, s1, per1 = cpu_sample(oracle, grid, nodes, path, frames[:1], 1, single_rows, 1)
+    return {"value": round(rays / secs / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"{min(bands, HEIGHT // rows)} bands of {rows} rows x {WIDTH} px per frame and traversal, "
+                      f"{len(frames)} frame(s) ({rays // (5 * len(frames))} rays per traversal per frame), "
+                      f"FP32 oracle restatement, one call per band",
+            "seconds": round(secs, 2),
+            "per_traversal": {t: (round(v, 4) if v else None) for t, v in per.items()},
+            "single_core": {"value": round(r1 / s1 / 1e6, 4), "cores": 1, "seconds": round(s1, 2),
+                            "sample": f"one band of {single_rows} rows of frame {frames[0]} per traversal",
+                            "per_traversal": {t: (round(v, 4) if v else None) for t, v in per1.items()}}}
 
 
 def run_reference(args):
@@ -188,19 +213,24 @@ def run_reference(args):
     nodes, st = oracle.build_svo(grid, "rope")
     path = cameras.ct_path(DIMS)
     threads = os.cpu_count() or 1
-    row_step = args.ref_row_step
     for fi in frame_indices(args.warmup, offset=7):
-        cpu_sample(oracle, grid, nodes, path, [fi], row_step * 4, threads)
+        cpu_sample(oracle, grid, nodes, path, [fi], 1, 16, threads)
     rays, secs, per = 0, 0.0, {}
     times = []
+    acc = {t: [0, 0.0] for t in TRAVERSALS}
     for fi in frame_indices(args.steps):
-        r, s, per = cpu_sample(oracle, grid, nodes, path, [fi], row_step, threads)
+        r, s, p = cpu_sample(oracle, grid, nodes, path, [fi], args.ref_bands, args.band_rows, threads)
         rays += r
         secs += s
         times.append(s)
+        for t in TRAVERSALS:
+            if p[t]:
+                acc[t][0] += r // len(TRAVERSALS)
+                acc[t][1] += (r // len(TRAVERSALS)) / (p[t] * 1e6)
+    per = {t: (v[0] / v[1] / 1e6 if v[1] else None) for t, v in acc.items()}
     value = rays / secs / 1e6
-    sample = (f"every {row_step}th row of {args.steps} frames x 5 traversals "
-              f"({rays // (5 * args.steps)} rays per traversal per frame)")
+    sample = (f"{args.ref_bands} bands of {args.band_rows} rows x {WIDTH} px of each of {args.steps} frames x 5 "
+              f"traversals ({rays // (5 * args.steps)} rays per traversal per frame), one oracle call per band")
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * secs / args.steps, 3),
@@ -752,12 +782,8 @@ def run_ours(args):
     if rank == 0 and not args.no_cpu_baseline:
         import oracle
         oracle.build()
-        threads = os.cpu_count() or 1
-        rays, secs, cper = cpu_sample(oracle, grid, nodes, path, frames[:1], args.cpu_row_step, threads)
-        line["cpu_baseline"] = {"value": round(rays / secs / 1e6, 4), "unit": "Mrays/s", "cores": threads,
-                                "kind": "port",
-                                "sample": f"every {args.cpu_row_step}th row of frame {frames[0]}, all 5 traversals "
-                                          f"({rays // 5} rays each), FP32 oracle restatement"}
+        line["cpu_baseline"] = cpu_baseline_line(oracle, grid, nodes, path, frames[:args.cpu_frames], args.cpu_bands,
+                                                 args.band_rows, args.single_core_rows)
     if rank == 0:
         print(json.dumps(line))
     ctx.close()
@@ -772,8 +798,11 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--cpu-row-step", type=int, default=20)
-    ap.add_argument("--ref-row-step", type=int, default=60)
+    ap.add_argument("--band-rows", type=int, default=64, help="rows per oracle call of the CPU legs")
+    ap.add_argument("--cpu-bands", type=int, default=4, help="bands per frame and traversal of cpu_baseline")
+    ap.add_argument("--cpu-frames", type=int, default=2, help="frames of cpu_baseline")
+    ap.add_argument("--single-core-rows", type=int, default=8, help="rows of the single-core cpu_baseline band")
+    ap.add_argument("--ref-bands", type=int, default=3, help="bands per frame and traversal of --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and serving measurements")
     ap.add_argument("--batched-size", type=int, default=1024)

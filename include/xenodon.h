@@ -160,6 +160,35 @@ XN_API int xn_render_device(xn_ctx* ctx, const xn_volume* vol, int traversal, co
                             const xn_params* params, void* d_rgba, float* d_emission,
                             uint32_t* d_loads, void* stream);
 
+/* An output region's render target with its host read-back buffer and its
+ * fence: the asynchronous form of xn_render, replacing HeadlessOutput's image,
+ * staging buffer and fence (src/backend/headless/HeadlessOutput.cpp:38-136).
+ * The read-back goes into pinned host memory with an asynchronous copy, so a
+ * caller renders the next frame into a second output while it encodes this
+ * one.
+ *   xn_output_create   an output of up to max_pixels pixels (device image,
+ *                      pinned host image, events, error word)
+ *   xn_output_render   queues the render of params->output_region (at most
+ *                      max_pixels pixels) on the context's stream, timed by
+ *                      events, then the copy into the pinned image (skipped
+ *                      with XN_OUTPUT_DISCARD, the reference's
+ *                      --discard-output); returns at once.  The previous
+ *                      render into this output must have been waited for.
+ *   xn_output_wait     the fence: blocks until the queued render and copy are
+ *                      done; *rgba (width*height*4 bytes, row pitch width*4)
+ *                      stays valid until the next xn_output_render on this
+ *                      output; *kernel_ms as xn_render.  Returns
+ *                      XN_ERR_RAY_LIMIT like xn_render.
+ * Outputs of one context share its stream, so their renders run in the order
+ * they were queued; waits may come from any thread. */
+typedef struct xn_output xn_output;
+#define XN_OUTPUT_DISCARD 1
+XN_API int xn_output_create(xn_ctx* ctx, uint64_t max_pixels, xn_output** out);
+XN_API int xn_output_render(xn_output* out, const xn_volume* vol, int traversal, const xn_camera* cam,
+                            const xn_params* params, int flags);
+XN_API int xn_output_wait(xn_output* out, const uint8_t** rgba, float* kernel_ms);
+XN_API int xn_output_destroy(xn_output* out);
+
 /* ---------------------------------------------------------- batching --- */
 
 /* One frame of a batch (no counterpart in the reference, which renders one
@@ -288,11 +317,15 @@ XN_API int xn_build_svo_volume(xn_ctx* ctx, const void* d_rgba, uint32_t dx, uin
  * 8-byte aligned) are the caller's device memory, and all scratch comes from one
  * fixed 32 MiB device array that every GPU loading the library holds until the
  * process exits.  A grid whose build needs more scratch than that (about 2
- * million voxels for sparse or rope trees, fewer for DAGs) is rejected with
- * XN_ERR_BUDGET before anything runs; a node buffer that is too small is rejected
- * with XN_ERR_ARG and stats->n_nodes set to the size needed.  Work is queued on
- * `stream` (a cudaStream_t of the current device) and the call returns once it is
- * done.  The first call on a device looks up the scratch array's device address,
+ * million voxels for sparse or rope trees) is rejected with XN_ERR_BUDGET before
+ * anything runs.  A DAG's deduplication buffers depend on the node count, so a
+ * DAG that outgrows the array is found, and rejected the same way, only after
+ * the bottom-up and top-down passes.  A node buffer that is too small is
+ * rejected with XN_ERR_ARG and stats->n_nodes set to the size needed.  Work is
+ * queued on `stream`, which must belong to the current device (XN_ERR_ARG
+ * otherwise), and the call returns once it is done.  The first call on a
+ * device, and the first after its context changed (another context made
+ * current, or the device reset), looks up the scratch array's device address,
  * so make that first call before any stream capture.  Every call reuses the
  * same array and clears what it needs; calls that overlap on the GPU race. */
 XN_API int xn_build_svo_static(const uint32_t* d_rgba, uint32_t dx, uint32_t dy, uint32_t dz, int type,
@@ -318,15 +351,18 @@ XN_API int xn_volume_load(xn_ctx* ctx, const char* path, xn_volume** out);
 /* Grid::load_tiff (src/model/Grid.cpp:27-79): a stacked TIFF, one page per z
  * slice, read the way TIFFReadRGBAImage hands it to the reference (rows
  * bottom-up, gray expanded to RGB, alpha 255 when absent, unassociated alpha
- * premultiplied).  Uncompressed 8-bit gray/RGB/RGBA, strips or tiles, classic
- * TIFF or BigTIFF.  *rgba_out is malloc'd (dims[0]*dims[1]*dims[2]*4 bytes,
+ * premultiplied).  8-bit gray/RGB/RGBA, strips or tiles, classic TIFF or
+ * BigTIFF; uncompressed, LZW, Deflate or PackBits, with or without the
+ * horizontal predictor.  *rgba_out is malloc'd (dims[0]*dims[1]*dims[2]*4 bytes,
  * x fastest); free it with xn_free. */
 XN_API int xn_tiff_load(const char* path, uint8_t** rgba_out, uint32_t dims_out[3]);
 /* Writes a grid as an uncompressed RGBA BigTIFF that xn_tiff_load (and
  * libtiff's TIFFReadRGBAImage) reads back unchanged. */
 XN_API int xn_tiff_save(const char* path, const uint8_t* rgba, uint32_t dx, uint32_t dy, uint32_t dz);
 /* HeadlessDisplay::save's PNG output (src/backend/headless/HeadlessDisplay.cpp:80-85):
- * width*height RGBA8 pixels, row-major, top row first. */
+ * width*height RGBA8 pixels, row-major, top row first.  Adaptive scanline
+ * filters and deflate (LZ77 + dynamic Huffman codes), the rows compressed in
+ * bands on the host's cores. */
 XN_API int xn_png_save(const char* path, const uint8_t* rgba, uint32_t width, uint32_t height);
 
 #endif

@@ -57,8 +57,9 @@ def build() -> None:
 
 def build_ref() -> bool:
     """Compile the reference's own builder when the reference checkout exists."""
-    ref = os.environ.get("XENODON_REFERENCE", "/root/reference")
-    if not (Path(ref) / "src" / "model" / "OctreeConstruction.h").exists():
+    ref = subprocess.run(["make", "-s", "-C", str(HERE), "--no-print-directory", "print-reference"],
+                         capture_output=True, text=True).stdout.strip()
+    if not ref or not (Path(ref) / "src" / "model" / "OctreeConstruction.h").exists():
         return False
     subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REFERENCE={ref}"], check=True)
     return True

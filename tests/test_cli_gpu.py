@@ -6,8 +6,6 @@ from __future__ import annotations
 import json
 import re
 import subprocess
-import struct
-import zlib
 from pathlib import Path
 
 import numpy as np
@@ -27,17 +25,8 @@ def run(*args, cwd):
 
 
 def png_pixels(path) -> np.ndarray:
-    data = Path(path).read_bytes()
-    pos, idat = 8, b""
-    while pos < len(data):
-        n, = struct.unpack(">I", data[pos:pos + 4])
-        t, c = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + n]
-        if t == b"IHDR":
-            w, h = struct.unpack(">II", c[:8])
-        elif t == b"IDAT":
-            idat += c
-        pos += 12 + n
-    return np.frombuffer(zlib.decompress(idat), np.uint8).reshape(h, w * 4 + 1)[:, 1:].reshape(h, w, 4)
+    from pngdec import decode
+    return decode(Path(path).read_bytes())
 
 
 @pytest.mark.parametrize("svo_type,flag", [("sparse", []), ("rope", ["--rope"]), ("dag", ["--dag"])])
@@ -134,6 +123,43 @@ def test_multi_region_composite_equals_single_region(ctx, tmp_path):
         c = png_pixels(tmp_path / f"two-{2 * i + 1}.png")
         assert np.array_equal(a, b) and np.array_equal(b, c)
     assert not (tmp_path / "two-6.png").exists()
+
+
+def test_pipelined_frames_equal_serial_frames(ctx, tmp_path):
+    """The headless loop queues frame n+1 before it saves frame n (two output
+    sets, a saver thread); XN_HEADLESS_SERIAL=1 renders, waits and saves one
+    frame at a time.  Both write the same files and the same stats lines, on
+    two regions and five frames."""
+    import os
+    import xenodon_gb300 as xg
+    from xenodon_gb300 import cameras, volumes
+    g = volumes.blobs(32, seed=7)
+    xg.tiff_save(tmp_path / "v.tif", g)
+    lines = [" ".join(f"{v:.6f}" for v in (*c[0], *c[1], *c[2]))
+             for c in cameras.orbit(np.array([0.5, 0.5, 0.5]), 2.0, 5)]
+    (tmp_path / "cam.txt").write_text("\n".join(lines) + "\n")
+    (tmp_path / "two.conf").write_text(
+        "device {\n vkindex = 0\n offset = (0, 0)\n extent = (40, 30)\n}\n"
+        "device {\n vkindex = 1\n offset = (40, 10)\n extent = (24, 30)\n}\n")
+    runs = {}
+    for mode in ("pipelined", "serial"):
+        env = dict(os.environ)
+        env.pop("XN_HEADLESS_SERIAL", None)
+        if mode == "serial":
+            env["XN_HEADLESS_SERIAL"] = "1"
+        p = subprocess.run([str(CLI_PATH), "render", "--headless", "two.conf", "v.tif", "--camera", "cam.txt",
+                            "-e", "10", "--output", mode + "-{}.png", "--stats-output", mode + ".txt"],
+                           capture_output=True, text=True, cwd=tmp_path, timeout=300, env=env)
+        assert p.returncode == 0, p.stdout
+        runs[mode] = p.stdout
+        assert sorted(int(m) for m in re.findall(r"Saved output to '" + mode + r"-(\d+)\.png'", p.stdout)) == \
+            list(range(5))
+    for i in range(5):
+        assert np.array_equal(png_pixels(tmp_path / f"pipelined-{i}.png"), png_pixels(tmp_path / f"serial-{i}.png"))
+    a = (tmp_path / "pipelined.txt").read_text().splitlines()
+    b = (tmp_path / "serial.txt").read_text().splitlines()
+    assert a[0] == b[0] == f"total rays: {5 * (40 * 30 + 24 * 30)}"
+    assert [ln.split(":")[0] for ln in a] == [ln.split(":")[0] for ln in b]
 
 
 def test_camera_script_errors(ctx, tmp_path):

@@ -249,22 +249,8 @@ def test_tiff_layer_size_check_follows_reference(built_library, tmp_path):
 
 
 def _png_decode(data: bytes) -> np.ndarray:
-    assert data[:8] == b"\x89PNG\r\n\x1a\n"
-    pos, idat = 8, b""
-    while pos < len(data):
-        n, = struct.unpack(">I", data[pos:pos + 4])
-        t, c = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + n]
-        crc, = struct.unpack(">I", data[pos + 8 + n:pos + 12 + n])
-        assert crc == zlib.crc32(t + c) & 0xFFFFFFFF
-        if t == b"IHDR":
-            w, h, depth, ctype = struct.unpack(">IIBB", c[:10])
-            assert (depth, ctype) == (8, 6)
-        elif t == b"IDAT":
-            idat += c
-        pos += 12 + n
-    raw = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(h, w * 4 + 1)
-    assert np.all(raw[:, 0] == 0)
-    return raw[:, 1:].reshape(h, w, 4)
+    from pngdec import decode
+    return decode(data)
 
 
 @pytest.mark.parametrize("shape", [(1, 1), (33, 47), (300, 251)])
@@ -273,6 +259,30 @@ def test_png_decodes_to_the_pixels(built_library, tmp_path, shape):
     img = np.random.default_rng(4).integers(0, 256, shape + (4,)).astype(np.uint8)
     xg.png_save(tmp_path / "f.png", img)
     assert np.array_equal(_png_decode((tmp_path / "f.png").read_bytes()), img)
+
+
+def test_png_compresses_a_rendered_frame(built_library, tmp_path):
+    """A frame-like image (black background, opaque alpha, a smooth disc and
+    noise) round-trips through zlib and compresses well below its raw size;
+    its rows span several parallel deflate bands."""
+    import xenodon_gb300 as xg
+    h, w = 720, 1280
+    yy, xx = np.mgrid[0:h, 0:w]
+    r = np.hypot(yy - h / 2, xx - w / 2)
+    img = np.zeros((h, w, 4), np.uint8)
+    img[..., 3] = 255
+    disc = r < 250
+    img[..., 0] = np.where(disc, (255 - r).clip(0, 255), 0).astype(np.uint8)
+    img[..., 1] = np.where(disc, (xx % 256), 0).astype(np.uint8)
+    rng = np.random.default_rng(1)
+    img[300:340, 100:400, 2] = rng.integers(0, 256, (40, 300))
+    xg.png_save(tmp_path / "f.png", img)
+    data = (tmp_path / "f.png").read_bytes()
+    assert np.array_equal(_png_decode(data), img)
+    assert len(data) < img.nbytes / 8
+    blank = np.zeros((64, 4000, 4), np.uint8)
+    xg.png_save(tmp_path / "b.png", blank)
+    assert np.array_equal(_png_decode((tmp_path / "b.png").read_bytes()), blank)
 
 
 @pytest.mark.parametrize("compression", [5, 8, 32946, 32773])

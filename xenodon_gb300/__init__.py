@@ -37,7 +37,7 @@ EXPORTS = (
     "xn_batch_graph_destroy", "xn_server_create", "xn_server_destroy", "xn_server_add_grid",
     "xn_server_add_svo", "xn_server_add_volume", "xn_server_submit", "xn_server_wait", "xn_server_stats",
     "xn_svo_load", "xn_svo_save", "xn_volume_save", "xn_volume_load", "xn_tiff_load", "xn_tiff_save",
-    "xn_png_save",
+    "xn_png_save", "xn_output_create", "xn_output_render", "xn_output_wait", "xn_output_destroy",
 )
 
 
@@ -152,6 +152,10 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "xn_tiff_load": (i32, [ctypes.c_char_p, P(P(ctypes.c_uint8)), P(u32 * 3)]),
         "xn_tiff_save": (i32, [ctypes.c_char_p, vp, u32, u32, u32]),
         "xn_png_save": (i32, [ctypes.c_char_p, vp, u32, u32]),
+        "xn_output_create": (i32, [vp, u64, P(vp)]),
+        "xn_output_render": (i32, [vp, vp, i32, P(Camera), P(Params), i32]),
+        "xn_output_wait": (i32, [vp, P(P(ctypes.c_uint8)), P(ctypes.c_float)]),
+        "xn_output_destroy": (i32, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(l, name)

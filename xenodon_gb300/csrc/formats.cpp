@@ -1,4 +1,4 @@
-// Host file formats: stacked TIFF volumes and PNG frames.
+// Host file formats: stacked TIFF volumes (PNG frames are in png.cpp).
 //
 // Stacked TIFF (Grid::load_tiff, src/model/Grid.cpp:27-79).  libtiff is not
 // available, so this is a reader of its own for the files the reference's
@@ -18,10 +18,7 @@
 // when both width and height differ, Grid.cpp:47); later layers must still
 // hold at least width*height pixels here, where the reference would read past
 // them.
-//
-// PNG: RGBA8, non-interlaced, deflate "stored" blocks (the reference uses
-// lodepng, src/backend/headless/HeadlessDisplay.cpp:80-85; any conforming
-// decoder reads the same pixels).
+
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -520,42 +517,6 @@ int decode_page(Reader& r, const Ifd& d, uint32_t width, uint32_t height, uint8_
     return XN_OK;
 }
 
-uint32_t crc_table[256];
-bool crc_ready = false;
-
-uint32_t crc32_update(uint32_t c, const uint8_t* p, size_t n) {
-    if (!crc_ready) {
-        for (uint32_t i = 0; i < 256; ++i) {
-            uint32_t v = i;
-            for (int k = 0; k < 8; ++k) v = (v & 1) ? 0xEDB88320u ^ (v >> 1) : v >> 1;
-            crc_table[i] = v;
-        }
-        crc_ready = true;
-    }
-    for (size_t i = 0; i < n; ++i) c = crc_table[(c ^ p[i]) & 0xFF] ^ (c >> 8);
-    return c;
-}
-
-void put_be32(std::vector<uint8_t>& v, uint32_t x) {
-    v.push_back((uint8_t)(x >> 24));
-    v.push_back((uint8_t)(x >> 16));
-    v.push_back((uint8_t)(x >> 8));
-    v.push_back((uint8_t)x);
-}
-
-bool write_chunk(std::FILE* f, const char* type, const std::vector<uint8_t>& data) {
-    std::vector<uint8_t> head;
-    put_be32(head, (uint32_t)data.size());
-    head.insert(head.end(), type, type + 4);
-    uint32_t c = crc32_update(0xFFFFFFFFu, reinterpret_cast<const uint8_t*>(type), 4);
-    c = crc32_update(c, data.data(), data.size()) ^ 0xFFFFFFFFu;
-    std::vector<uint8_t> tail;
-    put_be32(tail, c);
-    return std::fwrite(head.data(), 1, head.size(), f) == head.size() &&
-           (data.empty() || std::fwrite(data.data(), 1, data.size(), f) == data.size()) &&
-           std::fwrite(tail.data(), 1, 4, f) == 4;
-}
-
 }  // namespace
 
 XN_API int xn_tiff_load(const char* path, uint8_t** rgba_out, uint32_t dims_out[3]) {
@@ -673,61 +634,6 @@ XN_API int xn_tiff_save(const char* path, const uint8_t* rgba, uint32_t dx, uint
             ok = std::fwrite(src, 1, (size_t)dx * 4, f) == (size_t)dx * 4;
         }
     }
-    if (std::fclose(f) != 0) ok = false;
-    return ok ? XN_OK : fail(XN_ERR_IO, "'%s': write failed", path);
-}
-
-XN_API int xn_png_save(const char* path, const uint8_t* rgba, uint32_t width, uint32_t height) {
-    if (!path || !rgba) return fail(XN_ERR_ARG, "xn_png_save: NULL argument");
-    if (!width || !height) return fail(XN_ERR_ARG, "xn_png_save: empty image");
-    std::FILE* f = std::fopen(path, "wb");
-    if (!f) return fail(XN_ERR_IO, "Failed to open '%s'", path);
-    static const uint8_t sig[8] = {137, 80, 78, 71, 13, 10, 26, 10};
-    bool ok = std::fwrite(sig, 1, 8, f) == 8;
-    std::vector<uint8_t> ihdr;
-    put_be32(ihdr, width);
-    put_be32(ihdr, height);
-    ihdr.insert(ihdr.end(), {8, 6, 0, 0, 0});  // 8-bit RGBA, deflate, no filter method extras, no interlace
-    ok = ok && write_chunk(f, "IHDR", ihdr);
-    // zlib stream of stored blocks over the filtered scanlines (filter 0)
-    const uint64_t stride = (uint64_t)width * 4 + 1;
-    const uint64_t raw = stride * height;
-    std::vector<uint8_t> z;
-    z.reserve(raw + raw / 65535 * 5 + 16);
-    z.push_back(0x78);
-    z.push_back(0x01);
-    uint32_t s1 = 1, s2 = 0;
-    uint64_t pos = 0;
-    std::vector<uint8_t> line(stride);
-    uint64_t in_block = 0;
-    size_t block_len_at = 0;
-    for (uint32_t y = 0; y < height; ++y) {
-        line[0] = 0;
-        std::memcpy(&line[1], rgba + (uint64_t)y * width * 4, (size_t)width * 4);
-        for (uint64_t i = 0; i < stride; ++i) {
-            if (in_block == 0) {
-                const uint64_t left = raw - pos;
-                const uint16_t len = (uint16_t)(left < 65535 ? left : 65535);
-                z.push_back(left <= 65535 ? 1 : 0);
-                block_len_at = z.size();
-                z.push_back((uint8_t)len);
-                z.push_back((uint8_t)(len >> 8));
-                z.push_back((uint8_t)~len);
-                z.push_back((uint8_t)(~len >> 8));
-                in_block = len;
-            }
-            const uint8_t b = line[i];
-            z.push_back(b);
-            s1 = (s1 + b) % 65521;
-            s2 = (s2 + s1) % 65521;
-            --in_block;
-            ++pos;
-        }
-    }
-    (void)block_len_at;
-    put_be32(z, (s2 << 16) | s1);
-    ok = ok && write_chunk(f, "IDAT", z);
-    ok = ok && write_chunk(f, "IEND", {});
     if (std::fclose(f) != 0) ok = false;
     return ok ? XN_OK : fail(XN_ERR_IO, "'%s': write failed", path);
 }

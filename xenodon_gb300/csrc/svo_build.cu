@@ -32,6 +32,8 @@
 #include <new>
 #include <vector>
 
+#include <cuda.h>  // CUcontext / CUresult types; the two driver calls are looked up at run time
+
 #include "../../include/xenodon.h"
 #include "xn_ctx.h"
 #include "xn_internal.h"
@@ -1285,11 +1287,48 @@ namespace {
 
 constexpr int STATIC_MAX_DEVICES = 64;
 std::mutex g_static_mu;
-void* g_static_scratch[STATIC_MAX_DEVICES];
+struct StaticScratch {
+    void* ptr = nullptr;
+    unsigned long long ctx_id = 0;  // the context the address belongs to (0: none yet)
+};
+StaticScratch g_static_scratch[STATIC_MAX_DEVICES];
 
-// Device address of the scratch array on the current device.  The first call
-// on a device looks it up with cudaGetSymbolAddress (host code must not use
-// the array's name as an address).
+// The driver's context identity, looked up through the runtime so that the
+// library needs no link against the driver library.  A context that is
+// destroyed and created again (cudaDeviceReset by this process, whichever
+// runtime makes the call) gets a new id, so an address looked up in the old
+// context is never reused.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+int current_context_id(unsigned long long* id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static int looked_up = 0;  // guarded by g_static_mu
+    if (!looked_up) {
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+        if (e == cudaSuccess) e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (e != cudaSuccess) return cuda_fail(e, "xn_build_svo_static: driver entry points");
+        if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return fail(XN_ERR_CUDA, "xn_build_svo_static: the driver has no cuCtxGetCurrent/cuCtxGetId");
+        get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+        get_id = reinterpret_cast<CtxGetIdFn>(f2);
+        looked_up = 1;
+    }
+    CUcontext c = nullptr;
+    if (get_current(&c) != CUDA_SUCCESS) return fail(XN_ERR_CUDA, "xn_build_svo_static: cuCtxGetCurrent failed");
+    *id = 0;
+    if (c && get_id(c, id) != CUDA_SUCCESS) return fail(XN_ERR_CUDA, "xn_build_svo_static: cuCtxGetId failed");
+    return XN_OK;
+}
+
+// Device address of the scratch array in the current device's context.  Host
+// code must not use the array's name as an address: the set-up looks it up
+// with cudaGetSymbolAddress, once per device and context (the first call on a
+// device, and the first after that device's context was reset).
 int static_scratch_address(void** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -1297,13 +1336,33 @@ int static_scratch_address(void** out) {
     if (dev < 0 || dev >= STATIC_MAX_DEVICES)
         return fail(XN_ERR_ARG, "xn_build_svo_static: device %d is beyond the %d supported", dev, STATIC_MAX_DEVICES);
     std::lock_guard<std::mutex> lk(g_static_mu);
-    if (!g_static_scratch[dev]) {
+    unsigned long long id = 0;
+    int r = current_context_id(&id);
+    if (r) return r;
+    StaticScratch& s = g_static_scratch[dev];
+    if (!s.ptr || id == 0 || s.ctx_id != id) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, xn_static_build_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "xn_build_svo_static: cudaGetSymbolAddress");
-        g_static_scratch[dev] = p;
+        // the lookup makes the device's primary context current if none was
+        if (id == 0 && (r = current_context_id(&id))) return r;
+        s.ptr = p;
+        s.ctx_id = id;
     }
-    *out = g_static_scratch[dev];
+    *out = s.ptr;
+    return XN_OK;
+}
+
+// The kernels run on the caller's stream and use the scratch array of the
+// current device, so the stream must belong to that device.
+int check_stream_device(cudaStream_t s) {
+    int dev = 0, sdev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaStreamGetDevice(s, &sdev);
+    if (e != cudaSuccess) return cuda_fail(e, "xn_build_svo_static: stream device");
+    if (sdev != dev)
+        return fail(XN_ERR_ARG, "xn_build_svo_static: the stream belongs to device %d, the current device is %d", sdev,
+                    dev);
     return XN_OK;
 }
 
@@ -1392,6 +1451,7 @@ int build_static(const uint32_t* d_vox, uint32_t dx, uint32_t dy, uint32_t dz, i
     std::memset(stats, 0, sizeof *stats);
     stats->side = side;
     if (L >= MAX_LEVELS) return fail(XN_ERR_ARG, "xn_build_svo_static: grid too large");
+    if (int rs = check_stream_device(s)) return rs;
     GridDev g{d_vox, dx, dy, dz};
     if (L == 0) {
         stats->total_leaves = stats->unique_leaves = stats->total_nodes = stats->n_nodes = 1;

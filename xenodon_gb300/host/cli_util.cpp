@@ -383,9 +383,12 @@ std::string fmt_double(double v) {
 }
 
 void Logger::log(const std::string& msg) {
+    std::lock_guard<std::mutex> lk(mu);  // the frame-saving thread logs too
     std::time_t t = std::time(nullptr);
     char ts[32];
-    std::strftime(ts, sizeof ts, "[%H:%M:%S] ", std::localtime(&t));
+    std::tm tmv{};
+    localtime_r(&t, &tmv);
+    std::strftime(ts, sizeof ts, "[%H:%M:%S] ", &tmv);
     std::string line = std::string(ts) + msg;
     if (console) std::cout << line << '\n' << std::flush;
     if (sink) *sink << line << '\n' << std::flush;

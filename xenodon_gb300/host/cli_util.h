@@ -6,6 +6,7 @@
 #include <functional>
 #include <ostream>
 #include <stdexcept>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -101,6 +102,7 @@ std::string fmt_double(double v);
 struct Logger {
     bool console = true;
     std::ostream* sink = nullptr;  // --log-output file, truncated when opened
+    std::mutex mu;
     void log(const std::string& msg);
 };
 

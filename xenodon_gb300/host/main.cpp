@@ -13,14 +13,17 @@
 // does; the exit status is 1 after an error (the reference always exits 0).
 #include <algorithm>
 #include <chrono>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <iostream>
 #include <memory>
+#include <mutex>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <xenodon.h>
@@ -220,6 +223,147 @@ struct FrameStats {
     double mrays() const { return (double)total_rays / (total * 1000.0); }
 };
 
+std::string output_name(const std::string& pattern, uint64_t frame) {
+    try {
+        return cli::format_frame_name(pattern, frame);
+    } catch (const cli::Error& e) {
+        throw cli::Error(std::string("Failed to format output filename: ") + e.what());
+    }
+}
+
+// The frames in flight of a headless run: `depth` sets of one xn_output per
+// device region, and one thread that composites a finished frame's regions
+// into the enclosing rectangle (opaque black where no region is, like
+// HeadlessDisplay::save, HeadlessDisplay.cpp:56-92) and writes its PNG.
+class FramePipeline {
+public:
+    FramePipeline(xn_ctx* ctx, const std::vector<cli::HeadlessDevice>& devices, int depth, cli::Rect enclosing,
+                  cli::Logger& log)
+        : devices_(devices), enclosing_(enclosing), log_(log), busy_(depth, false) {
+        outputs_.assign((size_t)depth, std::vector<xn_output*>(devices.size(), nullptr));
+        try {
+            for (auto& set : outputs_)
+                for (size_t i = 0; i < devices.size(); ++i)
+                    check(xn_output_create(ctx, (uint64_t)devices[i].region.width * devices[i].region.height, &set[i]));
+        } catch (...) {
+            for (auto& set : outputs_)
+                for (xn_output* o : set) xn_output_destroy(o);
+            throw;
+        }
+        saver_ = std::thread([this] { save_loop(); });
+    }
+    ~FramePipeline() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        if (saver_.joinable()) saver_.join();
+        for (auto& set : outputs_)
+            for (xn_output* o : set) xn_output_destroy(o);
+    }
+    xn_output* output(int set, size_t i) { return outputs_[(size_t)set][i]; }
+
+    // Blocks until the frame last rendered into `set` has been saved.
+    void acquire(int set) {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return !busy_[(size_t)set]; });
+    }
+
+    // Waits for the regions of `frame` (rendered into `set`), returns its
+    // stats, and hands the pixels to the saver unless `path` is empty.
+    FrameStats finish(uint64_t frame, int set, const std::string& path) {
+        FrameStats fs;
+        fs.min = 1.7976931348623157e308;
+        std::vector<const uint8_t*> px(devices_.size(), nullptr);
+        for (size_t i = 0; i < devices_.size(); ++i) {
+            float ms = 0;
+            int r = xn_output_wait(outputs_[(size_t)set][i], &px[i], &ms);
+            if (r == XN_ERR_RAY_LIMIT)
+                log_.log("Warning: frame " + std::to_string(frame) + ", device " + std::to_string(i) + ": " +
+                         xn_last_error() + "; the frame is saved as rendered");
+            else
+                check(r);
+            fs.total_rays += (uint64_t)devices_[i].region.width * devices_[i].region.height;
+            fs.outputs += 1;
+            fs.total += ms;
+            fs.max = std::max(fs.max, (double)ms);
+            fs.min = std::min(fs.min, (double)ms);
+        }
+        if (!path.empty()) {
+            std::lock_guard<std::mutex> lk(mu_);
+            busy_[(size_t)set] = true;
+            jobs_.push_back(Job{frame, path, std::move(px), set});
+            cv_.notify_all();
+        }
+        return fs;
+    }
+
+    // Blocks until every handed-over frame is saved.
+    void drain() {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] {
+            if (!jobs_.empty()) return false;
+            for (bool b : busy_)
+                if (b) return false;
+            return true;
+        });
+    }
+
+private:
+    struct Job {
+        uint64_t frame;
+        std::string path;
+        std::vector<const uint8_t*> pixels;
+        int set;
+    };
+
+    void save_loop() {
+        std::vector<uint8_t> image;
+        for (;;) {
+            Job job;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return stop_ || !jobs_.empty(); });
+                if (jobs_.empty()) return;
+                job = std::move(jobs_.front());
+                jobs_.erase(jobs_.begin());
+            }
+            log_.log("Saving frame " + std::to_string(job.frame) + "...");
+            image.assign((size_t)enclosing_.width * enclosing_.height * 4, 0);
+            for (size_t q = 0; q < image.size(); q += 4) image[q + 3] = 0xFF;  // 0xFF000000: opaque black
+            for (size_t i = 0; i < devices_.size(); ++i) {
+                const cli::Rect& rg = devices_[i].region;
+                const size_t sx = (size_t)((int64_t)rg.x - enclosing_.x), sy = (size_t)((int64_t)rg.y - enclosing_.y);
+                for (uint32_t y = 0; y < rg.height; ++y)
+                    std::memcpy(&image[((sy + y) * enclosing_.width + sx) * 4], job.pixels[i] + (size_t)y * rg.width * 4,
+                                (size_t)rg.width * 4);
+            }
+            log_.log("Compressing...");
+            if (xn_png_save(job.path.c_str(), image.data(), enclosing_.width, enclosing_.height) != XN_OK)
+                log_.log(std::string("Error saving output: ") + xn_last_error());
+            else
+                log_.log("Saved output to '" + job.path + "'");
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                busy_[(size_t)job.set] = false;
+            }
+            cv_.notify_all();
+        }
+    }
+
+    const std::vector<cli::HeadlessDevice>& devices_;
+    cli::Rect enclosing_;
+    cli::Logger& log_;
+    std::vector<std::vector<xn_output*>> outputs_;
+    std::vector<bool> busy_;
+    std::vector<Job> jobs_;
+    std::mutex mu_;
+    std::condition_variable cv_;
+    bool stop_ = false;
+    std::thread saver_;
+};
+
 std::string stats_text(const std::vector<FrameStats>& frames, double wall_s) {
     // RenderStatsAccumulator::save (src/render/RenderStats.cpp:127-158)
     uint64_t rays = 0;
@@ -343,9 +487,21 @@ int render(const std::vector<std::string>& args) {
         cli::CameraScript script(o.camera);
 
         const cli::Rect enclosing = cli::rect_union_composite(regions);
-        std::vector<std::vector<uint8_t>> pixels(devices.size());
-        for (size_t i = 0; i < devices.size(); ++i)
-            pixels[i].resize((size_t)devices[i].region.width * devices[i].region.height * 4);
+        for (const auto& d : devices) {
+            const cli::Rect& rg = d.region;
+            int64_t sx = (int64_t)rg.x - enclosing.x, sy = (int64_t)rg.y - enclosing.y;
+            if (sx < 0 || sy < 0 || sx + rg.width > enclosing.width || sy + rg.height > enclosing.height)
+                throw cli::Error("the device regions do not fit the composite image");
+        }
+        // Two sets of outputs: frame n renders into set n % 2 while the saver
+        // thread composites and encodes frame n-1 from the other set's pinned
+        // read-back (HeadlessDisplay::swap_buffers and save,
+        // HeadlessDisplay.cpp:39-92, moved off the render loop).
+        // XN_HEADLESS_SERIAL=1 keeps one set: each frame is rendered, waited
+        // for and saved before the next is queued, as the reference does.
+        const char* serial_env = std::getenv("XN_HEADLESS_SERIAL");
+        const int depth = serial_env && serial_env[0] == '1' ? 1 : 2;
+        FramePipeline pipe(ctx, devices, depth, enclosing, log);
         std::vector<FrameStats> frames;
         auto start = std::chrono::steady_clock::now();
         auto fps_start = start;
@@ -359,8 +515,8 @@ int render(const std::vector<std::string>& args) {
             std::memcpy(cam.forward, c.forward, sizeof cam.forward);
             std::memcpy(cam.up, c.up, sizeof cam.up);
             std::memcpy(cam.translation, c.translation, sizeof cam.translation);
-            FrameStats fs;
-            fs.min = 1.7976931348623157e308;
+            const int set = (int)(frame_no % (uint64_t)depth);
+            pipe.acquire(set);  // its previous frame is saved
             for (size_t i = 0; i < devices.size(); ++i) {
                 xn_params p;
                 p.output_region = {devices[i].region.x, devices[i].region.y, devices[i].region.width,
@@ -368,44 +524,23 @@ int render(const std::vector<std::string>& args) {
                 p.display_region = {display.x, display.y, display.width, display.height};
                 for (int k = 0; k < 3; ++k) p.voxel_ratio[k] = o.ratio[k];
                 p.emission_coeff = (float)o.emission;
-                float ms = 0;
-                int r = xn_render(ctx, vol, shader->traversal, &cam, &p, pixels[i].data(), nullptr, &ms);
-                if (r != XN_OK && r != XN_ERR_RAY_LIMIT) check(r);
-                fs.total_rays += (uint64_t)devices[i].region.width * devices[i].region.height;
-                fs.outputs += 1;
-                fs.total += ms;
-                fs.max = std::max(fs.max, (double)ms);
-                fs.min = std::min(fs.min, (double)ms);
+                check(xn_output_render(pipe.output(set, i), vol, shader->traversal, &cam, &p,
+                                       o.discard ? XN_OUTPUT_DISCARD : 0));
             }
-            // HeadlessDisplay::swap_buffers / save (HeadlessDisplay.cpp:39-92)
-            if (!o.discard) {
-                std::string path;
-                try {
-                    path = cli::format_frame_name(o.output, frame_no);
-                } catch (const cli::Error& e) {
-                    throw cli::Error(std::string("Failed to format output filename: ") + e.what());
-                }
-                log.log("Saving frame " + std::to_string(frame_no) + "...");
-                std::vector<uint8_t> image((size_t)enclosing.width * enclosing.height * 4, 0);
-                for (size_t q = 0; q < image.size(); q += 4) image[q + 3] = 0xFF;  // 0xFF000000: opaque black
-                for (size_t i = 0; i < devices.size(); ++i) {
-                    const cli::Rect& rg = devices[i].region;
-                    int64_t sx = (int64_t)rg.x - enclosing.x, sy = (int64_t)rg.y - enclosing.y;
-                    if (sx < 0 || sy < 0 || sx + rg.width > enclosing.width || sy + rg.height > enclosing.height)
-                        throw cli::Error("the device regions do not fit the composite image");
-                    for (uint32_t y = 0; y < rg.height; ++y)
-                        std::memcpy(&image[(((size_t)(sy + y)) * enclosing.width + (size_t)sx) * 4],
-                                    &pixels[i][(size_t)y * rg.width * 4], (size_t)rg.width * 4);
-                }
-                log.log("Compressing...");
-                if (xn_png_save(path.c_str(), image.data(), enclosing.width, enclosing.height) != XN_OK)
-                    log.log(std::string("Error saving output: ") + xn_last_error());
-                else
-                    log.log("Saved output to '" + path + "'");
+            // finish the frame before this one (or this one, with one set)
+            if (depth == 1) {
+                frames.push_back(pipe.finish(frame_no, set, o.discard ? "" : output_name(o.output, frame_no)));
+            } else if (frame_no > 0) {
+                frames.push_back(pipe.finish(frame_no - 1, 1 - set,
+                                             o.discard ? "" : output_name(o.output, frame_no - 1)));
+            }
+            const bool last = total_frames % o.repeat == 0 && script.update();
+            if (last) {
+                if (depth == 2) frames.push_back(pipe.finish(frame_no, set, o.discard ? "" : output_name(o.output, frame_no)));
+                ++frame_no;
+                break;
             }
             ++frame_no;
-            frames.push_back(fs);
-            if (total_frames % o.repeat == 0 && script.update()) break;
             auto now = std::chrono::steady_clock::now();
             double dt = std::chrono::duration<double>(now - fps_start).count();
             if (dt > 5.0) {
@@ -414,6 +549,7 @@ int render(const std::vector<std::string>& args) {
                 fps_start = now;
             }
         }
+        pipe.drain();
         double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
         uint64_t rays = 0;
         double total = 0;
