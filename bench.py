@@ -298,16 +298,17 @@ def measure_batched(ctx, xg, args):
     plain_ms = timed(plain)
     plain_out = [b.clone() for b in bufs[:: max(1, len(bufs) // 8)]]
     jobs = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs, bufs))
-    # tune the launch shape on a slice of the batch
-    k = min(16, len(specs))
-    tune_jobs = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs[::len(specs) // k], bufs))
-    best, _ = ctx.autotune_batch(tune_jobs, k, sptr)
-    graph = ctx.batch_graph(len(specs), best, sptr)
+    # the autotuner samples the whole batch, then times its finalists on all of it
+    best, _ = ctx.autotune_batch(jobs, len(specs), sptr)
     for b in bufs:
         b.fill_(-1)
-    batched_ms = timed(lambda: graph.launch(jobs, len(specs)))
+    if best.tile_width:  # a persistent-kernel shape: replayed as a CUDA graph
+        graph = ctx.batch_graph(len(specs), best, sptr)
+        batched_ms = timed(lambda: graph.launch(jobs, len(specs)))
+        graph.close()
+    else:  # the plain form won
+        batched_ms = timed(lambda: ctx.render_batch(jobs, len(specs), best, sptr))
     same = all(torch.equal(a, b) for a, b in zip(plain_out, bufs[:: max(1, len(bufs) // 8)]))
-    graph.close()
     small = batched_small_frames(ctx, xg, vol, timed, args)
     args.residents.append({"grid": grid_vol, "svo": vol, "dims": (n, n, n), "rope": True})
     return {
@@ -465,9 +466,7 @@ def measure_c3(ctx, xg, args):
         keep = [b.clone() for b in bufs[::4]]
         jobs = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs, bufs))
         untuned_ms = timed(lambda: ctx.render_batch(jobs, len(specs), xg.BatchConfig(8, 128, 0, 1), sptr), reps=1)
-        k = min(4, len(specs))
-        tune = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs[:: len(specs) // k], bufs))
-        best, _ = ctx.autotune_batch(tune, k, sptr)
+        best, _ = ctx.autotune_batch(jobs, len(specs), sptr)
         for b in bufs:
             b.fill_(-1)
         tuned_ms = timed(lambda: ctx.render_batch(jobs, len(specs), best, sptr))

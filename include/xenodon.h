@@ -128,6 +128,23 @@ XN_API int xn_volume_upload_grid(xn_ctx* ctx, const uint8_t* rgba, uint32_t dx, 
  * device for traversal. */
 XN_API int xn_volume_upload_svo(xn_ctx* ctx, const uint32_t* nodes, uint64_t n_nodes, uint64_t side,
                                 xn_volume** out);
+/* xn_volume_upload_svo with a choice of node format (the plugin boundary's
+ * node_fmt):
+ *   XN_NODES_U32  the reference's nodes, 10 little-endian u32 (as above);
+ *   XN_NODES_U64  72-byte nodes: the eight child indices as u64, then the u32
+ *                 colour and the u32 is_leaf_depth -- the reference's node
+ *                 with 64-bit indices, for trees of 2^32 nodes or more (no
+ *                 counterpart in the reference, whose indices are u32,
+ *                 src/model/OctreeConstruction.h:74-76).  Such an array does
+ *                 not fit in HBM: it is read twice from host memory in chunks
+ *                 and only the device layout is kept (36 bytes per internal
+ *                 node, at most 2^31 - 1 of them).  Rope words are not
+ *                 converted: svo-rope is refused on the volume.
+ * 8-byte aligned host memory. */
+#define XN_NODES_U32 0
+#define XN_NODES_U64 1
+XN_API int xn_volume_upload_svo_fmt(xn_ctx* ctx, const void* nodes, uint64_t n_nodes, uint64_t side, int node_fmt,
+                                    xn_volume** out);
 /* xn_volume_upload_grid from a grid already in device memory (no host copy). */
 XN_API int xn_volume_upload_grid_device(xn_ctx* ctx, const void* d_rgba, uint32_t dx, uint32_t dy, uint32_t dz,
                                         xn_volume** out);
@@ -202,9 +219,12 @@ typedef struct {
     void* d_rgba;
 } xn_job;
 
-/* Launch shape of the persistent batch kernel. */
+/* Launch shape of the persistent batch kernel, or (tile_width XN_BATCH_PLAIN)
+ * the plain form: each job through the single-frame kernels, one launch per
+ * frame, in order. */
+#define XN_BATCH_PLAIN 0
 typedef struct {
-    uint32_t tile_width;    /* warp tile width in pixels: 4, 8, 16 or 32 (height = 32/width) */
+    uint32_t tile_width;    /* warp tile width in pixels: 4, 8, 16 or 32 (height = 32/width); 0: plain */
     uint32_t block_threads; /* threads per block: a multiple of 32, at most 1024 */
     uint32_t blocks_per_sm; /* resident blocks per SM; 0 = as many as fit */
     uint32_t chunk;         /* warp tiles a warp takes per pop of the work queue; 0: no queue, a grid of
@@ -219,8 +239,10 @@ typedef struct {
  * with no queue. */
 XN_API int xn_render_batch(xn_ctx* ctx, const xn_job* jobs, int n_jobs, const xn_batch_config* cfg, void* stream);
 
-/* Times xn_render_batch over a sweep of launch shapes on the given jobs and
- * keeps the fastest for their mix of traversals (used when cfg is NULL). */
+/* Times xn_render_batch over a sweep of launch shapes, the plain form among
+ * them, on the given jobs and keeps the fastest for their mix of traversals
+ * (used when cfg is NULL): every shape once on up to 8 jobs spread over the
+ * batch, then the three fastest and the plain form twice on the whole batch. */
 XN_API int xn_autotune_batch(xn_ctx* ctx, const xn_job* jobs, int n_jobs, void* stream, xn_batch_config* best,
                              float* best_ms);
 
@@ -307,6 +329,26 @@ XN_API void xn_free(void* p);
 #define XN_BUILD_LEAN 0x100
 XN_API int xn_build_svo_volume(xn_ctx* ctx, const void* d_rgba, uint32_t dx, uint32_t dy, uint32_t dz, int type,
                                int heuristic, double threshold, xn_volume** out, xn_build_stats* stats);
+
+/* Supplies the part of a grid inside a box: nx*ny*nz RGBA8 texels starting at
+ * (x0, y0, z0), x fastest, into rgba.  Returns 0, or non-zero to stop the
+ * build (which then fails with XN_ERR_IO). */
+typedef int (*xn_region_reader)(void* user, uint32_t x0, uint32_t y0, uint32_t z0, uint32_t nx, uint32_t ny,
+                                uint32_t nz, uint8_t* rgba);
+
+/* build_octree + save_svo (src/model/OctreeConstruction.h:197-237,
+ * src/model/Octree.cpp:96-114) for grids that are never resident on the device
+ * as a whole: the sparse octree of a dx*dy*dz grid, built one top-level cube
+ * (side/2 on each axis) at a time from the texels `read` supplies, each cube's
+ * nodes written to out_path as they are done.  The file is byte-identical to
+ * xn_build_svo + xn_svo_save of the whole grid (the reference's node order is
+ * the root followed by the eight cubes' own trees, each rebased by the node
+ * count before it).  The device holds one cube's grid, build scratch and nodes
+ * at a time.  Sparse trees only: ropes and DAG deduplication relate nodes of
+ * different cubes.  Fails with XN_ERR_FORMAT past 2^32 nodes (the format's
+ * 32-bit indices). */
+XN_API int xn_build_svo_streamed(xn_ctx* ctx, uint32_t dx, uint32_t dy, uint32_t dz, int heuristic, double threshold,
+                                 xn_region_reader read, void* user, const char* out_path, xn_build_stats* stats);
 
 /* No counterpart in the reference.  The same octree build as xn_build_svo, for
  * callers that cannot allocate device memory: code that runs inside another

@@ -51,6 +51,29 @@ def test_convert_writes_the_reference_bytes(ctx, tmp_path, svo_type, flag):
     assert f" Perfect tree nodes: {perfect}\n" in out
 
 
+def test_convert_streamed_writes_the_reference_bytes(ctx, tmp_path):
+    """`convert --streamed` (one top-level octant at a time on the device)
+    writes the reference builder's own bytes for every sparse golden file."""
+    import xenodon_gb300 as xg
+    z = np.load(GOLDEN)
+    meta = json.loads(bytes(z["meta"]).decode())
+    done = 0
+    for m in meta:
+        if m["type"] != "sparse":
+            continue
+        xg.tiff_save(tmp_path / "in.tif", z["grid__" + m["grid"]])
+        flag = ["--chan-diff", str(m["threshold"])] if m["heuristic"] == "chan-diff" else \
+            ["--std-dev", repr(float(m["threshold"]))]
+        rc, out = run("convert", "--streamed", *flag, "in.tif", "out.svo", cwd=tmp_path)
+        assert rc == 0, out
+        assert (tmp_path / "out.svo").read_bytes() == bytes(z[m["key"]]), m["key"]
+        assert f" Unique nodes: {m['stats']['n_nodes']} (" in out
+        done += 1
+    assert done >= 5
+    rc, out = run("convert", "--streamed", "--rope", "in.tif", "out.svo", cwd=tmp_path)
+    assert rc == 1 and "--streamed builds a sparse tree" in out
+
+
 def test_convert_std_dev(ctx, tmp_path):
     import xenodon_gb300 as xg
     z = np.load(GOLDEN)

@@ -37,7 +37,7 @@ EXPORTS = (
     "xn_batch_graph_destroy", "xn_server_create", "xn_server_destroy", "xn_server_add_grid",
     "xn_server_add_svo", "xn_server_add_volume", "xn_server_submit", "xn_server_wait", "xn_server_stats",
     "xn_svo_load", "xn_svo_save", "xn_volume_save", "xn_volume_load", "xn_tiff_load", "xn_tiff_save",
-    "xn_png_save", "xn_output_create", "xn_output_render", "xn_output_wait", "xn_output_destroy",
+    "xn_png_save", "xn_build_svo_streamed", "xn_volume_upload_svo_fmt", "xn_output_create", "xn_output_render", "xn_output_wait", "xn_output_destroy",
 )
 
 
@@ -100,6 +100,9 @@ class BuildStats(ctypes.Structure):
                 ("side", ctypes.c_uint64), ("n_nodes", ctypes.c_uint64)]
 
 
+REGION_READER = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                 ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint8))
+
 _lib = None
 
 
@@ -152,6 +155,9 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "xn_tiff_load": (i32, [ctypes.c_char_p, P(P(ctypes.c_uint8)), P(u32 * 3)]),
         "xn_tiff_save": (i32, [ctypes.c_char_p, vp, u32, u32, u32]),
         "xn_png_save": (i32, [ctypes.c_char_p, vp, u32, u32]),
+        "xn_build_svo_streamed": (i32, [vp, u32, u32, u32, i32, ctypes.c_double, REGION_READER, vp,
+                                        ctypes.c_char_p, P(BuildStats)]),
+        "xn_volume_upload_svo_fmt": (i32, [vp, vp, u64, u64, i32, P(vp)]),
         "xn_output_create": (i32, [vp, u64, P(vp)]),
         "xn_output_render": (i32, [vp, vp, i32, P(Camera), P(Params), i32]),
         "xn_output_wait": (i32, [vp, P(P(ctypes.c_uint8)), P(ctypes.c_float)]),
@@ -170,6 +176,16 @@ def _check(code: int) -> int:
     if code != XN_OK:
         raise XenodonError(code, load_library().xn_last_error().decode(errors="replace"))
     return code
+
+
+def nodes_to_u64(nodes: np.ndarray) -> np.ndarray:
+    """The reference's (n, 10) u32 nodes in the 64-bit node form (n, 72) u8."""
+    n = np.ascontiguousarray(nodes, dtype=np.uint32).reshape(-1, 10)
+    out = np.zeros((n.shape[0], 18), np.uint32)
+    out[:, 0:16:2] = n[:, :8]  # little-endian u64: low words
+    out[:, 16] = n[:, 8]
+    out[:, 17] = n[:, 9]
+    return out.view(np.uint8).reshape(-1, 72)
 
 
 def make_camera(forward, up, translation) -> Camera:
@@ -299,6 +315,15 @@ class Context:
         _check(self.lib.xn_volume_upload_svo(self.handle, n.ctypes.data, n.shape[0], int(side), ctypes.byref(h)))
         return Volume(self, h)
 
+    def upload_svo64(self, nodes64: np.ndarray, side: int) -> Volume:
+        """nodes64: the 64-bit node form, a structured or uint8 array of 72-byte
+        nodes (eight u64 child indices, u32 colour, u32 is_leaf_depth)."""
+        raw = np.ascontiguousarray(nodes64).view(np.uint8).reshape(-1, 72)
+        h = ctypes.c_void_p()
+        _check(self.lib.xn_volume_upload_svo_fmt(self.handle, raw.ctypes.data, raw.shape[0], int(side), 1,
+                                                 ctypes.byref(h)))
+        return Volume(self, h)
+
     def render(self, vol: Volume, traversal, camera: Camera, params: Params, emission: bool = False,
                allow_ray_limit: bool = False, out: np.ndarray | None = None):
         """Render to host memory.  Returns (rgba (h, w, 4) u8, emission (h, w, 3) f32 or None, kernel_ms).
@@ -367,6 +392,33 @@ class Context:
         finally:
             self.lib.xn_free(out)
         return arr, {f: int(getattr(st, f)) for f, _ in BuildStats._fields_}
+
+    def build_svo_streamed(self, dims, read_region, path, heuristic="chan-diff", threshold=0.0) -> dict:
+        """Sparse octree of a dx*dy*dz grid built one top-level cube at a time
+        and written to `path` (an XNDN-SVO file).  read_region(x0, y0, z0, nx,
+        ny, nz) returns that box as a uint8 (nz, ny, nx, 4) array.  Returns the
+        build stats."""
+        failure = []
+
+        def cb(_user, x0, y0, z0, nx, ny, nz, dst):
+            try:
+                box = np.ascontiguousarray(read_region(x0, y0, z0, nx, ny, nz), dtype=np.uint8)
+                if box.shape != (nz, ny, nx, 4):
+                    raise ValueError(f"read_region returned {box.shape}, wanted {(nz, ny, nx, 4)}")
+                ctypes.memmove(dst, box.ctypes.data, box.nbytes)
+                return 0
+            except Exception as exc:  # reported after the build returns
+                failure.append(exc)
+                return 1
+
+        fn = REGION_READER(cb)
+        st = BuildStats()
+        r = self.lib.xn_build_svo_streamed(self.handle, dims[0], dims[1], dims[2], HEURISTICS[heuristic],
+                                           float(threshold), fn, None, str(path).encode(), ctypes.byref(st))
+        if failure:
+            raise failure[0]
+        _check(r)
+        return {f: int(getattr(st, f)) for f, _ in BuildStats._fields_}
 
 
 class BatchGraph:

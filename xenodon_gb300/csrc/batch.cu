@@ -1,6 +1,7 @@
 // Batched rendering: job tables, the persistent launch, CUDA-graph replay and
 // the launch-shape autotuner.  (No counterpart in the reference, which renders
 // one frame per dispatch, src/render/Renderer.cpp:74-89.)
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -24,8 +25,9 @@ uint32_t traversal_mask(const xn_job* jobs, int n) {
 }
 
 int check_config(const xn_batch_config& c) {
+    if (c.tile_width == XN_BATCH_PLAIN) return XN_OK;  // one single-frame launch per job
     if (c.tile_width != 4 && c.tile_width != 8 && c.tile_width != 16 && c.tile_width != 32)
-        return fail(XN_ERR_ARG, "batch: tile_width must be 4, 8, 16 or 32");
+        return fail(XN_ERR_ARG, "batch: tile_width must be 4, 8, 16 or 32 (or 0, one launch per frame)");
     if (c.block_threads == 0 || c.block_threads % 32 || c.block_threads > 1024)
         return fail(XN_ERR_ARG, "batch: block_threads must be a multiple of 32 up to 1024");
 
@@ -121,10 +123,30 @@ bool generic_forced() {
 
 int render_batch_one(Ctx* c, const xn_job* jobs, int n, const xn_batch_config& cfg, cudaStream_t s);
 
+// The plain form: every job through the single-frame kernels, one launch
+// each, in order on the stream (the reference's one dispatch per frame,
+// src/render/Renderer.cpp:74-89, with its launch shape and register budget).
+int render_plain(Ctx* c, const xn_job* jobs, int n, cudaStream_t s) {
+    for (int i = 0; i < n; ++i) {
+        if (!jobs[i].volume || !jobs[i].d_rgba) return fail(XN_ERR_ARG, "batch: job %d has no volume or output", i);
+        const Volume* v = reinterpret_cast<const Volume*>(jobs[i].volume);
+        if (v->ctx != c) return fail(XN_ERR_ARG, "batch: job %d uses a volume of another context", i);
+        RenderLaunch L;
+        int r = make_launch(v, jobs[i].traversal, &jobs[i].camera, &jobs[i].params, L);
+        if (r) return r;
+        L.d_rgba = jobs[i].d_rgba;
+        L.d_err_word = c->d_err;
+        cudaError_t e = launch_render(L, s);
+        if (e != cudaSuccess) return cuda_fail(e, "xn_render_batch: plain launch");
+    }
+    return XN_OK;
+}
+
 // A batch whose jobs need different kernel forms runs as one launch per form
 // (each specialised, each over its own jobs, in the stream's order); with
 // XN_BATCH_GENERIC=1 the generic form takes the whole batch in one launch.
 int render_batch_locked(Ctx* c, const xn_job* jobs, int n, const xn_batch_config& cfg, cudaStream_t s) {
+    if (cfg.tile_width == XN_BATCH_PLAIN) return render_plain(c, jobs, n, s);
     if (!generic_forced()) {
         std::vector<int> forms;
         int r = forms_of(c, jobs, n, forms);
@@ -211,6 +233,13 @@ XN_API int xn_render_batch(xn_ctx* h, const xn_job* jobs, int n, const xn_batch_
     return render_batch_locked(c, jobs, n, k, static_cast<cudaStream_t>(stream));
 }
 
+// Two rounds: every candidate launch shape -- the persistent kernel's tile /
+// block / queue shapes and the plain form, one single-frame launch per job --
+// is timed once on a sample of the jobs spread over the batch (at most 8), then
+// the four fastest, the plain form always among them, are timed twice on the
+// whole batch; the fastest of those wins.  The plain form being a finalist
+// means the tuned batch does not lose to one launch per frame, up to timing
+// noise.
 XN_API int xn_autotune_batch(xn_ctx* h, const xn_job* jobs, int n, void* stream, xn_batch_config* best,
                              float* best_ms) {
     if (!h || !jobs || n <= 0) return fail(XN_ERR_ARG, "xn_autotune_batch: no jobs");
@@ -222,33 +251,53 @@ XN_API int xn_autotune_batch(xn_ctx* h, const xn_job* jobs, int n, void* stream,
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
         return fail(XN_ERR_CUDA, "xn_autotune_batch: events");
-    const uint32_t tiles[] = {4, 8, 16, 32};
-    const uint32_t threads[] = {64, 128, 256};
-    const uint32_t chunks[] = {0, 1, 2, 4};  // 0: one warp per tile over a full grid, no queue
-    xn_batch_config winner = default_config();
+    std::vector<xn_batch_config> cand;
+    cand.push_back(xn_batch_config{XN_BATCH_PLAIN, 0, 0, 0});
+    for (uint32_t tw : {4u, 8u, 16u, 32u})
+        for (uint32_t bt : {64u, 128u, 256u})
+            for (uint32_t ch : {0u, 1u, 2u, 4u})  // 0: one warp per tile over a full grid, no queue
+                cand.push_back(xn_batch_config{tw, bt, 0, ch});
+    std::vector<xn_job> sample;
+    const int want = n < 8 ? n : 8;
+    for (int i = 0; i < want; ++i) sample.push_back(jobs[(int)((int64_t)i * n / want)]);
+    auto time_it = [&](const xn_batch_config& k, const xn_job* js, int m, int reps, float* ms_out) -> int {
+        int rr = render_batch_locked(c, js, m, k, s);  // warm-up
+        float best_t = 3.4e38f;
+        for (int i = 0; i < reps && !rr; ++i) {
+            cudaEventRecord(e0, s);
+            rr = render_batch_locked(c, js, m, k, s);
+            cudaEventRecord(e1, s);
+            float ms = 0;
+            if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+                rr = fail(XN_ERR_CUDA, "xn_autotune_batch: timing");
+            best_t = std::min(best_t, ms);
+        }
+        *ms_out = best_t;
+        return rr;
+    };
+    std::vector<std::pair<float, int>> score;
+    for (size_t i = 0; i < cand.size() && !r; ++i) {
+        float ms = 0;
+        r = time_it(cand[i], sample.data(), (int)sample.size(), 1, &ms);
+        score.emplace_back(ms, (int)i);
+    }
+    xn_batch_config winner = cand[0];
     float winner_ms = 3.4e38f;
-    for (uint32_t tw : tiles)
-        for (uint32_t bt : threads)
-            for (uint32_t ch : chunks) {
-                xn_batch_config k{tw, bt, 0, ch};
-                if ((r = render_batch_locked(c, jobs, n, k, s))) break;  // warm-up
-                float total = 0;
-                const int reps = 3;
-                for (int i = 0; i < reps && !r; ++i) {
-                    cudaEventRecord(e0, s);
-                    r = render_batch_locked(c, jobs, n, k, s);
-                    cudaEventRecord(e1, s);
-                    float ms = 0;
-                    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
-                        r = fail(XN_ERR_CUDA, "xn_autotune_batch: timing");
-                    total += ms;
-                }
-                if (r) break;
-                if (total / reps < winner_ms) {
-                    winner_ms = total / reps;
-                    winner = k;
-                }
+    if (!r) {
+        std::sort(score.begin(), score.end());
+        std::vector<int> finalists;
+        for (size_t i = 0; i < score.size() && finalists.size() < 3; ++i)
+            if (score[i].second != 0) finalists.push_back(score[i].second);
+        finalists.push_back(0);  // the plain form
+        for (int idx : finalists) {
+            float ms = 0;
+            if ((r = time_it(cand[idx], jobs, n, 2, &ms))) break;
+            if (ms < winner_ms) {
+                winner_ms = ms;
+                winner = cand[idx];
             }
+        }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (r) return r;
@@ -316,6 +365,10 @@ XN_API int xn_batch_graph_create(xn_ctx* h, int capacity, const xn_batch_config*
     g->ctx = c;
     g->stream = static_cast<cudaStream_t>(stream);
     g->cfg = cfg ? *cfg : default_config();
+    if (g->cfg.tile_width == XN_BATCH_PLAIN) {
+        delete g;
+        return fail(XN_ERR_ARG, "xn_batch_graph_create: the plain form (one launch per frame) is not captured");
+    }
     if (g->cfg.chunk == 0) g->cfg.chunk = 1;  // the tile count changes per replay: graphs use the queue form
     g->capacity = capacity;
     g->split = !generic_forced();

@@ -27,10 +27,14 @@
 // children of in-grid ones.
 #include <cstdint>
 #include <cstdlib>
+#include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <algorithm>
 #include <new>
 #include <vector>
+
+#include <unistd.h>
 
 #include <cuda.h>  // CUcontext / CUresult types; the two driver calls are looked up at run time
 
@@ -742,9 +746,11 @@ int exclusive_scan(Scratch& sc, const In* in, uint64_t n, unsigned* out, cudaStr
 // n_nodes*10 words owned by the caller through ctx->device_free.
 int build_svo_device(Ctx* c, const uint32_t* d_vox, uint32_t dx, uint32_t dy, uint32_t dz, int type, int heuristic,
                      double threshold, uint32_t** d_nodes, uint64_t* d_nodes_bytes, xn_build_stats* stats,
-                     Volume* lean) {
+                     Volume* lean, SubBuild* sub) {
     cudaStream_t s = c->stream;
-    const uint64_t side = std::max(ceil_pow2(dx), std::max(ceil_pow2(dy), ceil_pow2(dz)));
+    const uint64_t fit = std::max(ceil_pow2(dx), std::max(ceil_pow2(dy), ceil_pow2(dz)));
+    const uint64_t side = sub ? sub->side : fit;
+    const int depth_off = sub ? sub->depth_offset : 0;
     int L = 0;
     while ((1ull << L) < side) ++L;
     GridDev g{d_vox, dx, dy, dz};
@@ -753,6 +759,9 @@ int build_svo_device(Ctx* c, const uint32_t* d_vox, uint32_t dx, uint32_t dy, ui
     *d_nodes = nullptr;
     *d_nodes_bytes = 0;
     if (L >= MAX_LEVELS) return fail(XN_ERR_ARG, "xn_build_svo: grid too large");
+    if (sub && (side < fit || (side & (side - 1)) || L == 0 || lean || type != XN_SVO_SPARSE))
+        return fail(XN_ERR_ARG, "xn_build_svo: invalid cube build (side %llu for a %ux%ux%u grid)",
+                    (unsigned long long)side, dx, dy, dz);
     if (lean && L == 0) return LEAN_LEAF_ROOT;
 
     if (L == 0) {  // a single voxel: the root is a depth-0 leaf
@@ -876,6 +885,9 @@ int build_svo_device(Ctx* c, const uint32_t* d_vox, uint32_t dx, uint32_t dy, ui
         if ((e = cudaGetLastError()) != cudaSuccess) break;
     }
     if (e != cudaSuccess) return cuda_fail(e, "xn_build_svo: bottom-up pass");
+    if (sub && (e = cudaMemcpyAsync(sub->root_stats, stats_buf[0], stat_bytes, cudaMemcpyDeviceToHost, s)) !=
+                   cudaSuccess)
+        return cuda_fail(e, "xn_build_svo: root statistics");
 
     unsigned long long n_total = 0;
     if ((e = cudaMemcpyAsync(&n_total, size[0], 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
@@ -974,7 +986,7 @@ int build_svo_device(Ctx* c, const uint32_t* d_vox, uint32_t dx, uint32_t dy, ui
         a.cur = geo[d];
         a.child_is_voxel = d == L - 1;
         if (d < L - 1) a.child = geo[d + 1];
-        a.depth = d;
+        a.depth = d + depth_off;
         a.n_total = n_total;
         a.size = size[d];
         a.child_size = d < L - 1 ? size[d + 1] : nullptr;
@@ -1261,6 +1273,300 @@ XN_API int xn_build_svo_volume(xn_ctx* h, const void* d_rgba, uint32_t dx, uint3
         return r;
     }
     *out = reinterpret_cast<xn_volume*>(v);
+    return XN_OK;
+}
+
+// ----------------------------------------------------------- streamed build ---
+//
+// xn_build_svo_streamed: the sparse octree of a grid that is never resident on
+// the device as a whole.  The reference's node order is the reverse of a
+// post-order build (OctreeConstruction.h:92-112): the root, then the subtree
+// of child 7, then child 6's, ..., child 0's, each laid out the same way, with
+// child indices absolute.  So the tree is the root followed by the eight
+// top-level cubes' own trees (cube k at origin (k>>2 & 1, k>>1 & 1, k & 1) *
+// side/2), each built alone -- the same kernels over the cube's part of the
+// grid, with the cube's side and its root one level down -- and rebased by the
+// number of nodes before it: one running sum over the cubes' sizes.  A cube
+// outside the grid is a black leaf (OctreeConstruction.h:146-154).  The root's
+// decision and colour (OctreeConstruction.h:141-181) come from the cubes' root
+// statistics: sums, byte minima and maxima, or exact moments.  Ropes and DAG
+// deduplication relate nodes of different cubes and are not part of it.
+
+namespace xn {
+namespace {
+
+static_assert(sizeof(CDStats) <= sizeof(SubBuild::root_stats) && sizeof(SDStats) <= sizeof(SubBuild::root_stats),
+              "root statistics fit the cube build's buffer");
+
+__global__ void rebase_kernel(uint32_t* nodes, uint64_t n, uint32_t base) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        uint32_t* p = nodes + i * 10;
+        if (p[9] < LEAF)
+            for (int k = 0; k < 8; ++k) p[k] += base;
+    }
+}
+
+struct Out {
+    std::FILE* f = nullptr;
+    ~Out() {
+        if (f) std::fclose(f);
+    }
+};
+
+bool write_node_le(std::FILE* f, const uint32_t w[10]) {
+    unsigned char b[40];
+    for (int i = 0; i < 10; ++i)
+        for (int k = 0; k < 4; ++k) b[4 * i + k] = (unsigned char)(w[i] >> (8 * k));
+    return std::fwrite(b, 1, 40, f) == 40;
+}
+
+// Grid::stddev_scan's sequential double loop (Grid.cpp:193-203) over the whole
+// grid, z-slab by z-slab through the reader: the root's decision when the
+// exact moments leave it inside the rounding band.
+int stddev_root_sequential(xn_region_reader read, void* user, uint32_t dx, uint32_t dy, uint32_t dz,
+                           const SDStats& st, double threshold, bool* split) {
+    const uint64_t n = (uint64_t)dx * dy * dz;
+    const double nd = (double)n;
+    double avg[4];
+    for (int c = 0; c < 4; ++c) avg[c] = (double)st.s1[c] / nd;
+    const uint32_t slab = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(dz, (64ull << 20) / ((uint64_t)dx * dy * 4)));
+    std::vector<uint8_t> buf;
+    double s = 0.0;
+    for (uint32_t z0 = 0; z0 < dz; z0 += slab) {
+        const uint32_t nz = std::min(slab, dz - z0);
+        buf.resize((uint64_t)dx * dy * nz * 4);
+        if (read(user, 0, 0, z0, dx, dy, nz, buf.data()) != 0)
+            return fail(XN_ERR_IO, "xn_build_svo_streamed: the reader failed at z %u", z0);
+        for (uint64_t i = 0; i < (uint64_t)dx * dy * nz; ++i) {
+            const uint8_t* v = &buf[4 * i];
+            const double d0 = (double)v[0] - avg[0], d1 = (double)v[1] - avg[1];
+            const double d2 = (double)v[2] - avg[2], d3 = (double)v[3] - avg[3];
+            s += ((d0 * d0 + d1 * d1) + d2 * d2) + d3 * d3;
+        }
+    }
+    *split = std::sqrt(s / nd) > threshold;
+    return XN_OK;
+}
+
+}  // namespace
+}  // namespace xn
+
+XN_API int xn_build_svo_streamed(xn_ctx* h, uint32_t dx, uint32_t dy, uint32_t dz, int heuristic, double threshold,
+                                 xn_region_reader read, void* user, const char* out_path, xn_build_stats* stats) {
+    if (!h || !read || !out_path || !stats) return fail(XN_ERR_ARG, "xn_build_svo_streamed: NULL argument");
+    if (!dx || !dy || !dz) return fail(XN_ERR_ARG, "xn_build_svo_streamed: empty grid %ux%ux%u", dx, dy, dz);
+    if (heuristic == XN_HEUR_CHANNEL_DIFF) {
+        if (!(threshold >= 0.0 && threshold <= 255.0) || threshold != (double)(int)threshold)
+            return fail(XN_ERR_ARG, "xn_build_svo_streamed: --chan-diff must be an integer in 0..255");
+    } else if (heuristic == XN_HEUR_STD_DEV) {
+        if (!(threshold >= 0.0)) return fail(XN_ERR_ARG, "xn_build_svo_streamed: --std-dev must be >= 0");
+    } else {
+        return fail(XN_ERR_ARG, "xn_build_svo_streamed: invalid heuristic %d", heuristic);
+    }
+    Ctx* c = reinterpret_cast<Ctx*>(h);
+    std::lock_guard<std::mutex> lk(c->mu);
+    int r = c->activate();
+    if (r) return r;
+    std::memset(stats, 0, sizeof *stats);
+    const uint64_t side = std::max(ceil_pow2(dx), std::max(ceil_pow2(dy), ceil_pow2(dz)));
+    stats->side = side;
+    Out out;
+    out.f = std::fopen(out_path, "wb");
+    if (!out.f) return fail(XN_ERR_IO, "Failed to open '%s'", out_path);
+    unsigned char head[24] = {'X', 'N', 'D', 'N', '-', 'S', 'V', 'O'};
+    auto put_header = [&](uint64_t n) {
+        for (int k = 0; k < 8; ++k) {
+            head[8 + k] = (unsigned char)(side >> (8 * k));
+            head[16 + k] = (unsigned char)(n >> (8 * k));
+        }
+        return std::fseek(out.f, 0, SEEK_SET) == 0 && std::fwrite(head, 1, 24, out.f) == 24;
+    };
+    if (side == 1) {  // one voxel: the root is that voxel's leaf
+        uint8_t v[4];
+        if (read(user, 0, 0, 0, 1, 1, 1, v) != 0) return fail(XN_ERR_IO, "xn_build_svo_streamed: the reader failed");
+        const uint32_t node[10] = {0, 0, 0, 0, 0, 0, 0, 0, (uint32_t)v[0] | v[1] << 8 | v[2] << 16 | (uint32_t)v[3] << 24,
+                                   LEAF};
+        if (!put_header(1) || !write_node_le(out.f, node)) return fail(XN_ERR_IO, "'%s': write failed", out_path);
+        stats->total_leaves = stats->unique_leaves = stats->total_nodes = stats->n_nodes = 1;
+        return XN_OK;
+    }
+    const uint64_t S = side / 2;
+    const uint32_t zero10[10] = {};
+    if (!put_header(0) || !write_node_le(out.f, zero10)) return fail(XN_ERR_IO, "'%s': write failed", out_path);
+
+    uint32_t root_ch[8] = {};
+    uint64_t next = 1, leaves = 0, depth = 0, count = 0;
+    unsigned long long sum[4] = {0, 0, 0, 0}, sq[4] = {0, 0, 0, 0};
+    uint32_t mn = 0xFFFFFFFFu, mx = 0;
+    std::vector<uint8_t> host;
+    std::vector<uint32_t> chunk;
+    cudaStream_t s = c->stream;
+    for (int k = 7; k >= 0; --k) {
+        const uint64_t ox = ((k >> 2) & 1) * S, oy = ((k >> 1) & 1) * S, oz = (k & 1) * S;
+        if (next > 0xFFFFFFFFull)
+            return fail(XN_ERR_FORMAT, "xn_build_svo_streamed: more than 2^32 nodes exceed the SVO format");
+        root_ch[k] = (uint32_t)next;
+        if (ox >= dx || oy >= dy || oz >= dz) {  // outside the grid: a black leaf one level down
+            const uint32_t node[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, LEAF | 1u};
+            if (!write_node_le(out.f, node)) return fail(XN_ERR_IO, "'%s': write failed", out_path);
+            next += 1;
+            leaves += 1;
+            depth = std::max<uint64_t>(depth, 1);
+            continue;
+        }
+        const uint32_t sx = (uint32_t)std::min<uint64_t>(S, dx - ox), sy = (uint32_t)std::min<uint64_t>(S, dy - oy),
+                       sz = (uint32_t)std::min<uint64_t>(S, dz - oz);
+        const uint64_t nvox = (uint64_t)sx * sy * sz;
+        try {
+            host.resize(nvox * 4);
+        } catch (const std::bad_alloc&) {
+            return fail(XN_ERR_NOMEM, "xn_build_svo_streamed: out of host memory");
+        }
+        if (read(user, (uint32_t)ox, (uint32_t)oy, (uint32_t)oz, sx, sy, sz, host.data()) != 0)
+            return fail(XN_ERR_IO, "xn_build_svo_streamed: the reader failed for the cube at (%llu, %llu, %llu)",
+                        (unsigned long long)ox, (unsigned long long)oy, (unsigned long long)oz);
+        count += nvox;
+        if (S == 1) {  // the cube is one voxel: a leaf one level down
+            const uint8_t* v = host.data();
+            const uint32_t w = (uint32_t)v[0] | v[1] << 8 | v[2] << 16 | (uint32_t)v[3] << 24;
+            const uint32_t node[10] = {0, 0, 0, 0, 0, 0, 0, 0, w, LEAF | 1u};
+            if (!write_node_le(out.f, node)) return fail(XN_ERR_IO, "'%s': write failed", out_path);
+            for (int ch = 0; ch < 4; ++ch) {
+                sum[ch] += v[ch];
+                sq[ch] += (unsigned long long)v[ch] * v[ch];
+            }
+            for (int b = 0; b < 4; ++b) {
+                const uint32_t sh = 8 * b;
+                const uint32_t lo = std::min((mn >> sh) & 0xFFu, (w >> sh) & 0xFFu);
+                const uint32_t hi = std::max((mx >> sh) & 0xFFu, (w >> sh) & 0xFFu);
+                mn = (mn & ~(0xFFu << sh)) | (lo << sh);
+                mx = (mx & ~(0xFFu << sh)) | (hi << sh);
+            }
+            next += 1;
+            leaves += 1;
+            depth = std::max<uint64_t>(depth, 1);
+            continue;
+        }
+        uint32_t* d_vox = nullptr;
+        if ((r = c->device_alloc(reinterpret_cast<void**>(&d_vox), nvox * 4, "xn_build_svo_streamed: cube grid")))
+            return r;
+        cudaError_t e = cudaMemcpyAsync(d_vox, host.data(), nvox * 4, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            c->device_free(d_vox, nvox * 4);
+            return cuda_fail(e, "xn_build_svo_streamed: cube upload");
+        }
+        SubBuild sub;
+        sub.side = S;
+        sub.depth_offset = 1;
+        xn_build_stats st{};
+        uint32_t* d_nodes = nullptr;
+        uint64_t nbytes = 0;
+        r = build_svo_device(c, d_vox, sx, sy, sz, XN_SVO_SPARSE, heuristic, threshold, &d_nodes, &nbytes, &st, nullptr,
+                             &sub);
+        c->device_free(d_vox, nvox * 4);
+        if (r) return r;
+        const uint64_t n = st.n_nodes;
+        if (next + n > 0x100000000ull) {
+            c->device_free(d_nodes, nbytes);
+            return fail(XN_ERR_FORMAT, "xn_build_svo_streamed: more than 2^32 nodes exceed the SVO format");
+        }
+        rebase_kernel<<<1024, 256, 0, s>>>(d_nodes, n, (uint32_t)next);
+        e = cudaGetLastError();
+        // the cube's nodes to the file, in chunks
+        const uint64_t CH = 1ull << 22;  // nodes per chunk
+        for (uint64_t off = 0; off < n && e == cudaSuccess; off += CH) {
+            const uint64_t take = std::min(CH, n - off);
+            chunk.resize(take * 10);
+            e = cudaMemcpyAsync(chunk.data(), d_nodes + off * 10, take * 40, cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e == cudaSuccess) {
+                for (uint64_t i = 0; i < take; ++i)
+                    if (!write_node_le(out.f, &chunk[i * 10])) {
+                        c->device_free(d_nodes, nbytes);
+                        return fail(XN_ERR_IO, "'%s': write failed", out_path);
+                    }
+            }
+        }
+        c->device_free(d_nodes, nbytes);
+        if (e != cudaSuccess) return cuda_fail(e, "xn_build_svo_streamed: cube nodes");
+        next += n;
+        leaves += st.total_leaves;
+        depth = std::max<uint64_t>(depth, st.depth);
+        if (heuristic == XN_HEUR_CHANNEL_DIFF) {
+            CDStats cs;
+            std::memcpy(&cs, sub.root_stats, sizeof cs);
+            for (int ch = 0; ch < 4; ++ch) sum[ch] += cs.sum[ch];
+            for (int b = 0; b < 4; ++b) {
+                const uint32_t sh = 8 * b;
+                const uint32_t lo = std::min((mn >> sh) & 0xFFu, (cs.mn >> sh) & 0xFFu);
+                const uint32_t hi = std::max((mx >> sh) & 0xFFu, (cs.mx >> sh) & 0xFFu);
+                mn = (mn & ~(0xFFu << sh)) | (lo << sh);
+                mx = (mx & ~(0xFFu << sh)) | (hi << sh);
+            }
+        } else {
+            SDStats ss;
+            std::memcpy(&ss, sub.root_stats, sizeof ss);
+            for (int ch = 0; ch < 4; ++ch) {
+                sum[ch] += ss.s1[ch];
+                sq[ch] += ss.s2[ch];
+            }
+        }
+    }
+    // the root (OctreeConstruction.h:141-181): partly outside -> split;
+    // fully inside -> the heuristic on the whole grid
+    const bool fully = dx == side && dy == side && dz == side;
+    uint32_t avg = 0;
+    bool split = true;
+    if (heuristic == XN_HEUR_CHANNEL_DIFF) {
+        for (int ch = 0; ch < 4; ++ch) avg |= (uint32_t)(uint8_t)(sum[ch] / count) << (8 * ch);
+        uint32_t maxdiff = 0;
+        for (int b = 0; b < 4; ++b) {
+            const uint32_t hi = (mx >> (8 * b)) & 0xFFu, lo = (mn >> (8 * b)) & 0xFFu;
+            maxdiff = std::max(maxdiff, hi > lo ? hi - lo : 0u);
+        }
+        split = maxdiff > (uint32_t)threshold;
+    } else {
+        const double nd = (double)count;
+        unsigned __int128 E = 0;
+        for (int ch = 0; ch < 4; ++ch) {
+            avg |= (uint32_t)(uint8_t)((double)sum[ch] / nd) << (8 * ch);
+            E += (unsigned __int128)count * sq[ch] - (unsigned __int128)sum[ch] * sum[ch];
+        }
+        if (E == 0) {
+            split = 0.0 > threshold;
+        } else {
+            const double sd = std::sqrt((double)E / (nd * nd));
+            const double band = (nd + 16.0) * 2.220446049250313e-16 * sd + 1e-300;
+            split = sd > threshold;
+            if (fully && std::fabs(sd - threshold) <= band) {
+                SDStats all{};
+                for (int ch = 0; ch < 4; ++ch) {
+                    all.s1[ch] = sum[ch];
+                    all.s2[ch] = sq[ch];
+                }
+                if ((r = stddev_root_sequential(read, user, dx, dy, dz, all, threshold, &split))) return r;
+            }
+        }
+    }
+    if (fully && !split) {  // the whole grid is one leaf
+        const uint32_t node[10] = {0, 0, 0, 0, 0, 0, 0, 0, avg, LEAF};
+        if (!put_header(1) || !write_node_le(out.f, node) || std::fflush(out.f) != 0 ||
+            ftruncate(fileno(out.f), 64) != 0)
+            return fail(XN_ERR_IO, "'%s': write failed", out_path);
+        stats->total_leaves = stats->unique_leaves = stats->total_nodes = stats->n_nodes = 1;
+        return XN_OK;
+    }
+    uint32_t root[10];
+    for (int k = 0; k < 8; ++k) root[k] = root_ch[k];
+    root[8] = avg;
+    root[9] = 0;
+    if (!put_header(next) || !write_node_le(out.f, root) || std::fflush(out.f) != 0)
+        return fail(XN_ERR_IO, "'%s': write failed", out_path);
+    stats->total_leaves = stats->unique_leaves = leaves;
+    stats->total_nodes = stats->n_nodes = next;
+    stats->depth = depth;
     return XN_OK;
 }
 

@@ -168,6 +168,28 @@ __global__ void check_layout_kernel(const uint32_t* inner, const uint32_t* depth
 }
 
 }  // namespace
+
+// Checks a compact-layout volume's arrays on the device (every index in
+// range) and records whether its depth fields match the tree.
+int validate_compact_layout(Ctx* c, Volume* v, const char* what) {
+    uint32_t* flags = nullptr;
+    uint32_t hf[2] = {1, 1};
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&flags), 8, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, 8, c->stream);
+    if (e == cudaSuccess) {
+        check_layout_kernel<<<1024, 256, 0, c->stream>>>(v->inner, v->inner_depth, v->rinner, v->leaves, v->n_inner,
+                                                           v->rinner ? v->n_leaves : 0, flags);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hf, flags, 8, cudaMemcpyDeviceToHost, c->stream);
+    if (flags) cudaFreeAsync(flags, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    if (hf[0]) return fail(XN_ERR_FORMAT, "%s: an index is out of range", what);
+    v->depth_consistent = hf[1] == 0;
+    return XN_OK;
+}
+
 }  // namespace xn
 
 using namespace xn;
@@ -298,21 +320,7 @@ XN_API int xn_volume_load(xn_ctx* h, const char* path, xn_volume** out) {
                       (r = stream_in(c->stream, st, in.f, v->leaves, hd.n_leaves * 32, path))))
             return drop(r);
     }
-    uint32_t* flags = nullptr;
-    uint32_t hf[2] = {1, 1};
-    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&flags), 8, c->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, 8, c->stream);
-    if (e == cudaSuccess) {
-        check_layout_kernel<<<1024, 256, 0, c->stream>>>(v->inner, v->inner_depth, v->rinner, v->leaves, hd.n_inner,
-                                                           hd.n_leaves, flags);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(hf, flags, 8, cudaMemcpyDeviceToHost, c->stream);
-    if (flags) cudaFreeAsync(flags, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess) return drop(cuda_fail(e, "xn_volume_load"));
-    if (hf[0]) return drop(fail(XN_ERR_FORMAT, "'%s': an index is out of range", path));
-    v->depth_consistent = hf[1] == 0;
+    if ((r = validate_compact_layout(c, v, path))) return drop(r);
     v->layout = XN_LAYOUT_COMPACT;
     if ((r = measure_inner_depth(c, v))) return drop(r);
     *out = reinterpret_cast<xn_volume*>(v);

@@ -87,15 +87,28 @@ int build_svo_layout(Ctx* c, Volume* v);
 // Sets v->max_inner_depth from the internal nodes' depth fields when the tree
 // is depth-consistent (svo_layout.cu).
 int measure_inner_depth(Ctx* c, Volume* v);
+// Range-checks a compact-layout volume's arrays on the device and sets its
+// depth_consistent flag (volume_io.cu).
+int validate_compact_layout(Ctx* c, Volume* v, const char* what);
 
 // Octree build on the device (svo_build.cu).  With lean == nullptr: the
 // reference node array in *d_nodes.  With lean: only the device layout's
 // inner / inner_depth arrays, written into *lean (sparse trees; no rope
 // records); returns LEAN_LEAF_ROOT when the root is a leaf (no internal nodes).
 constexpr int LEAN_LEAF_ROOT = 1;
+// A build of one cube of a larger tree (the streamed convert): the cube's
+// side (a power of two at least the grid's dims, where the grid is the part of
+// the whole grid inside the cube), the depth of its root in the whole tree,
+// and on return the root cell's scan statistics (the heuristic's statistics
+// struct, at most 64 bytes) for the decision of the whole tree's root.
+struct SubBuild {
+    uint64_t side = 0;
+    int depth_offset = 0;
+    unsigned char root_stats[64] = {};
+};
 int build_svo_device(Ctx* c, const uint32_t* d_vox, uint32_t dx, uint32_t dy, uint32_t dz, int type, int heuristic,
                      double threshold, uint32_t** d_nodes, uint64_t* d_nodes_bytes, xn_build_stats* stats,
-                     Volume* lean = nullptr);
+                     Volume* lean = nullptr, SubBuild* sub = nullptr);
 
 int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
 int cuda_fail(cudaError_t e, const char* what);

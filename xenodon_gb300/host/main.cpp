@@ -81,7 +81,10 @@ const char* HELP_CONVERT =
     "  --std-dev <x>     Merge a region when the standard deviation of its\n"
     "                    colours is at most x.\n"
     "  --lean            (.svc, sparse trees) Build straight into the device\n"
-    "                    layout, never holding the node array; not for svo-rope.\n";
+    "                    layout, never holding the node array; not for svo-rope.\n"
+    "  --streamed        (.svo, sparse trees) Build one top-level octant of the\n"
+    "                    grid at a time on the device, writing its nodes as they\n"
+    "                    are done; the same file as the whole-grid build.\n";
 
 const char* HELP_HEADLESS =
     "The headless configuration lists the output regions:\n"
@@ -583,13 +586,30 @@ int render(const std::vector<std::string>& args) {
     return 0;
 }
 
+// The streamed build's region reader over a grid in host memory.
+struct HostGrid {
+    const uint8_t* rgba;
+    uint32_t dx, dy, dz;
+};
+
+int read_host_region(void* user, uint32_t x0, uint32_t y0, uint32_t z0, uint32_t nx, uint32_t ny, uint32_t nz,
+                     uint8_t* out) {
+    const HostGrid* g = static_cast<const HostGrid*>(user);
+    if ((uint64_t)x0 + nx > g->dx || (uint64_t)y0 + ny > g->dy || (uint64_t)z0 + nz > g->dz) return 1;
+    for (uint32_t z = 0; z < nz; ++z)
+        for (uint32_t y = 0; y < ny; ++y)
+            std::memcpy(out + (((uint64_t)z * ny + y) * nx) * 4,
+                        g->rgba + ((((uint64_t)(z0 + z) * g->dy) + (y0 + y)) * g->dx + x0) * 4, (size_t)nx * 4);
+    return 0;
+}
+
 int convert(const std::vector<std::string>& args) {
     std::string src, dst;
-    bool dag = false, rope = false, lean = false;
+    bool dag = false, rope = false, lean = false, streamed = false;
     int64_t chan = -1;
     double sd = -1;
     cli::Command cmd;
-    cmd.flags = {{&dag, "--dag"}, {&rope, "--rope"}, {&lean, "--lean"}};
+    cmd.flags = {{&dag, "--dag"}, {&rope, "--rope"}, {&lean, "--lean"}, {&streamed, "--streamed"}};
     cmd.parameters = {
         {[&](const std::string& a) {
              uint64_t v;
@@ -627,6 +647,10 @@ int convert(const std::vector<std::string>& args) {
         std::printf("Error: --lean builds a sparse tree into a .svc file (no --dag or --rope)\n");
         return 1;
     }
+    if (streamed && (svc || dag || rope || lean)) {
+        std::printf("Error: --streamed builds a sparse tree into a .svo file (no --dag, --rope or --lean)\n");
+        return 1;
+    }
     std::printf("Loading source...\n");
     uint8_t* rgba = nullptr;
     uint32_t dim[3];
@@ -650,9 +674,13 @@ int convert(const std::vector<std::string>& args) {
         const int type = dag ? XN_SVO_DAG : rope ? XN_SVO_ROPE_TREE : XN_SVO_SPARSE;
         const int heur = sd >= 0 ? XN_HEUR_STD_DEV : XN_HEUR_CHANNEL_DIFF;
         const double thr = sd >= 0 ? sd : (double)std::max<int64_t>(chan, 0);
-        r = svc ? xn_build_svo_volume(ctx, rgba, dim[0], dim[1], dim[2], type | (lean ? XN_BUILD_LEAN : 0), heur, thr,
-                                      &vol, &st)
-                : xn_build_svo(ctx, rgba, dim[0], dim[1], dim[2], type, heur, thr, &nodes, &st);
+        HostGrid hg{rgba, dim[0], dim[1], dim[2]};
+        if (streamed)
+            r = xn_build_svo_streamed(ctx, dim[0], dim[1], dim[2], heur, thr, read_host_region, &hg, dst.c_str(), &st);
+        else
+            r = svc ? xn_build_svo_volume(ctx, rgba, dim[0], dim[1], dim[2], type | (lean ? XN_BUILD_LEAN : 0), heur,
+                                          thr, &vol, &st)
+                    : xn_build_svo(ctx, rgba, dim[0], dim[1], dim[2], type, heur, thr, &nodes, &st);
     }
     xn_free(rgba);
     if (r != XN_OK) {
@@ -679,7 +707,8 @@ int convert(const std::vector<std::string>& args) {
     std::printf(" Unique leaves: %llu\n", (unsigned long long)st.unique_leaves);
     std::printf(" Depth: %llu\n", (unsigned long long)st.depth);
     int rc = 0;
-    if ((svc ? xn_volume_save(ctx, vol, dst.c_str()) : xn_svo_save(dst.c_str(), nodes, st.n_nodes, st.side)) != XN_OK) {
+    if (!streamed &&
+        (svc ? xn_volume_save(ctx, vol, dst.c_str()) : xn_svo_save(dst.c_str(), nodes, st.n_nodes, st.side)) != XN_OK) {
         std::printf("Error writing '%s': %s\n", dst.c_str(), xn_last_error());
         rc = 1;
     }
