@@ -596,7 +596,7 @@ def measure_serving(ctx, xg, args, scene, residents):
         for arr, dur in zip(arrivals, durations):
             finish = max(finish, arr) + dur
             lat.append((finish - arr) * 1e3)
-        with xg.Server(ctx, hbm_budget=150 << 30, max_batch_jobs=64, streams=3) as srv:
+        with xg.Server(ctx, hbm_budget=150 << 30) as srv:
             for v, (kind, d) in host.items():
                 if kind == "grid":
                     srv.add_grid(v, d)
@@ -618,12 +618,110 @@ def measure_serving(ctx, xg, args, scene, residents):
             st = srv.stats()
         result["rates"].append({"offered_req_s": rate if rate > 0 else "closed", "p50_ms": round(st["p50_ms"], 3),
                                 "p99_ms": round(st["p99_ms"], 3), "mrays_s": round(st["mrays_per_s"], 1),
-                                "mean_batch": round(st["mean_batch"], 2), "identical_images": same,
+                                "mean_batch": round(st["mean_batch"], 2), "folded": st["folded"],
+                                "fold_launches": st["fold_launches"], "republished": st["republished"],
+                                "identical_images": same,
                                 "plain_p50_ms": round(float(np.percentile(lat, 50)), 3),
                                 "plain_p99_ms": round(float(np.percentile(lat, 99)), 3)})
     sat = max(r["mrays_s"] for r in result["rates"])
     result["served_vs_plain"] = round(sat / result["plain_mrays_s"], 3)
     return result
+
+
+def measure_svo_4k(ctx, xg, vol, n, trav, frames=4):
+    """One octree traversal at 3840x2160 on a resident n^3 gas-field octree
+    from `frames` orbit cameras at 2x the extent: Mrays/s, node words the
+    reference would read per ray, and those words' bytes per second."""
+    import torch
+    from xenodon_gb300 import cameras
+    w, h = 3840, 2160
+    params = xg.make_params(w, h, EMISSION)
+    cams = [xg.make_camera(*c) for c in cameras.orbit(np.array([0.5, 0.5, 0.5]), 2.0, frames)]
+    out = torch.empty((h, w), dtype=torch.int32, device="cuda")
+    loads = torch.empty((h, w), dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    ctx.render_device(vol, trav, cams[0], params, out.data_ptr(), None, None, sptr)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in cams]
+    for c, (a, b) in zip(cams, evs):
+        a.record(stream)
+        ctx.render_device(vol, trav, c, params, out.data_ptr(), None, None, sptr)
+        b.record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    words = 0
+    for c in cams:
+        ctx.render_device(vol, trav, c, params, out.data_ptr(), None, loads.data_ptr(), sptr)
+        words += int(loads.to(torch.int64).sum().item())
+    torch.cuda.synchronize()
+    rays = w * h * len(cams)
+    alg = 4.0 * words + 4.0 * rays
+    return {"workload": f"{trav}, {n}^3 gas-field octree, {w}x{h}, {len(cams)} orbit cameras at 2x the extent",
+            "ms_per_frame": round(ms / len(cams), 3), "mrays_s": round(rays / (ms * 1e3), 1),
+            "words_per_ray": round(words / rays, 1), "algorithmic_gbs": round(alg / (ms * 1e-3) / 1e9, 1)}
+
+
+def run_svo_4k_only(args):
+    """--svo-4k N: the lean sparse octree of the N^3 gas field (the seed-3
+    recipe), octree traversals at 3840x2160 (profiling the large-tree
+    traversals on a stand-in of the 2048^3 tree)."""
+    import torch
+    import xenodon_gb300 as xg
+    from xenodon_gb300 import build as native, volumes
+    native.build()
+    ctx = xg.Context(0)
+    n = args.svo_4k
+    g = volumes.gas_field(n, seed=3, device="cuda", as_tensor=True)
+    vol, st = ctx.build_svo_volume(g.data_ptr(), (n, n, n), "sparse", lean=True)
+    del g
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    line = {"octree_nodes": st["n_nodes"], "device_bytes": vol.info()["device_bytes"]}
+    for trav in args.svo_4k_traversals:
+        line[trav] = measure_svo_4k(ctx, xg, vol, n, trav)
+    print(json.dumps(line))
+    vol.release()
+    ctx.close()
+    return 0
+
+
+def run_batch_only(args):
+    """--batch-only: 512 frames of 256x256 (256 Fibonacci cameras, esvo and
+    svo-rope) of the CT volume's rope octree in one persistent launch per
+    traversal form (profiling the batch kernel on a small case)."""
+    import torch
+    import xenodon_gb300 as xg
+    from xenodon_gb300 import build as native, cameras, volumes
+    native.build()
+    ctx = xg.Context(0)
+    grid = volumes.ct_shell(*DIMS, seed=1, device="cuda")
+    nodes, st = ctx.build_svo(grid, "rope", "chan-diff", 0)
+    vol = ctx.upload_svo(nodes, st["side"])
+    w = h = 256
+    cams = cameras.fibonacci_sphere(256, cameras.volume_centre(DIMS), 1.8, cameras.forward_length_for_vfov(45.0, w, h))
+    params = xg.make_params(w, h, EMISSION)
+    specs = [(vol, t, xg.make_camera(*c), params) for t in ("esvo", "svo-rope") for c in cams]
+    bufs = [torch.empty((h, w), dtype=torch.int32, device="cuda") for _ in specs]
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    jobs = ctx.make_jobs((v, t, c, p, b.data_ptr()) for (v, t, c, p), b in zip(specs, bufs))
+    cfg = xg.BatchConfig(8, 256, 0, 1)
+    for _ in range(2):
+        ctx.render_batch(jobs, len(specs), cfg, sptr)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    ctx.render_batch(jobs, len(specs), cfg, sptr)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    print(json.dumps({"workload": "CT rope octree, esvo + svo-rope, 512 frames of 256x256, batch 8x4 tiles, "
+                                  "blocks of 256, queue chunk 1",
+                      "ms": round(ms, 3), "mrays_s": round(w * h * len(specs) / (ms * 1e3), 1)}))
+    vol.release()
+    ctx.close()
+    return 0
 
 
 def run_dda_4k_only(args):
@@ -635,7 +733,18 @@ def run_dda_4k_only(args):
     g = volumes.gas_field(args.dda_4k, seed=2, device="cuda", as_tensor=True)
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
-    print(json.dumps(measure_dda_4k(ctx, xg, g, args.dda_4k)))
+    line = {}
+    for form in args.dda_4k_forms:  # the grid's form on the device is chosen at upload
+        os.environ.pop("XN_GRID_LAYOUT", None)
+        os.environ.pop("XN_DDA_WARP_TILE", None)
+        if form in ("bricked", "linear"):
+            os.environ["XN_GRID_LAYOUT"] = form
+        elif form.startswith("texture-w"):
+            os.environ["XN_DDA_WARP_TILE"] = form[len("texture-w"):]
+        line[form] = measure_dda_4k(ctx, xg, g, args.dda_4k)
+    os.environ.pop("XN_GRID_LAYOUT", None)
+    os.environ.pop("XN_DDA_WARP_TILE", None)
+    print(json.dumps(line))
     ctx.close()
     return 0
 
@@ -809,6 +918,13 @@ def main(argv=None):
     ap.add_argument("--c3-size", type=int, default=2048, help="grid size of the large workload (0: skip it)")
     ap.add_argument("--dda-4k", type=int, default=0, metavar="N",
                     help="only the 3840x2160 DDA measurement on an N^3 gas field (for profiling); prints its line")
+    ap.add_argument("--dda-4k-forms", nargs="*", default=["texture"],
+                    help="grid forms for --dda-4k: texture, texture-w4/-w16/-w32 (warp tile width), bricked, linear")
+    ap.add_argument("--svo-4k", type=int, default=0, metavar="N",
+                    help="only octree traversals at 3840x2160 on the lean octree of an N^3 gas field (profiling)")
+    ap.add_argument("--svo-4k-traversals", nargs="*", default=["esvo"])
+    ap.add_argument("--batch-only", action="store_true",
+                    help="only the batch kernel on 512 frames of 256x256 of the CT octree (profiling)")
     ap.add_argument("--c3-frames", type=int, default=16)
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 200.0, 1000.0, 2000.0, 0.0])
@@ -817,6 +933,10 @@ def main(argv=None):
         return run_reference(args)
     if args.dda_4k:
         return run_dda_4k_only(args)
+    if args.svo_4k:
+        return run_svo_4k_only(args)
+    if args.batch_only:
+        return run_batch_only(args)
     return run_ours(args)
 
 

@@ -259,23 +259,33 @@ XN_API int xn_batch_graph_destroy(xn_batch_graph* g);
 
 /* A render server (no counterpart in the reference).  A worker thread keeps
  * registered volumes resident with least-recently-used eviction under an HBM
- * budget and admits requests in arrival order as memory allows.  Each
- * admitted set goes to one of `streams` CUDA streams: frames of 2^19 pixels or
- * more (each fills the GPU alone) through the single-frame kernels, the
- * smaller ones as one batch.  Newly arrived requests are admitted while
- * earlier batches still run.  A copy thread moves finished frames into the
- * callers' buffers. */
+ * budget (a volume is uploaded when it is registered, if it fits) and admits
+ * requests in arrival order as memory allows.  Frames below fold_max_pixels
+ * are folded into a persistent kernel while it runs: each is appended to a
+ * job ring in device memory that the kernel reads as it goes, on a
+ * high-priority stream, and copied out as soon as its own tiles are done.
+ * The kernel leaves after fold_idle_us without work (its waits are bounded)
+ * and is launched again when frames arrive.  Larger frames (each fills the GPU
+ * alone) run through the single-frame kernels on a low-priority stream, in
+ * bands of rows, `streams` of them in flight.  A copy thread moves finished
+ * frames into the callers' buffers. */
 typedef struct xn_server xn_server;
 typedef struct {
-    uint64_t hbm_budget; /* bytes for resident volumes and in-flight frames; 0 = the context's budget */
-    int max_batch_jobs;  /* requests per persistent launch (default 256) */
-    int streams;         /* batches in flight at once (default 3) */
+    uint64_t hbm_budget;   /* bytes for resident volumes and in-flight frames; 0 = the context's budget */
+    int max_batch_jobs;    /* job slots of a folding ring: frames one persistent launch takes (default 1024) */
+    int streams;           /* large frames in flight at once (default 2) */
+    uint64_t fold_max_pixels;    /* frames below this many pixels are folded (0: 2^19) */
+    uint32_t fold_idle_us;       /* the persistent kernel leaves after this long without work (0: 300) */
+    uint32_t fold_blocks_per_sm; /* its warps per SM in units of 8 (blocks of 128 threads), 1 or 2 (0: 1) */
 } xn_server_config;
 typedef struct {
     uint64_t completed, failed, batches, uploads, evictions, rays, hbm_used;
-    double mean_batch;   /* requests per batch */
+    double mean_batch;   /* requests per launch (persistent or single-frame) */
     double p50_ms, p99_ms, max_ms; /* submit -> result in host memory */
     double mrays_per_s;  /* rays of completed requests / time from the first submit to the last result */
+    uint64_t folded;         /* frames appended to a running or starting persistent kernel */
+    uint64_t fold_launches;  /* persistent kernel launches */
+    uint64_t republished;    /* frames that reached a ring after its kernel left, appended again */
 } xn_server_metrics;
 
 XN_API int xn_server_create(xn_ctx* ctx, const xn_server_config* cfg, xn_server** out);

@@ -190,6 +190,54 @@ def test_hbm_budget_refuses_uploads(built_library, blob_volumes):
         assert c.memory()[0] < g.nbytes // 2
 
 
+@pytest.mark.parametrize("cam", ["front", "inside", "grazing", "oblique"])
+def test_parity_dda_bricked_grid_layout(ctx, blob_volumes, monkeypatch, cam):
+    # XN_GRID_LAYOUT=bricked: 8^3 bricks of 2x2x1 16-byte groups, zero padding
+    import xenodon_gb300 as xg
+    g, _, _ = blob_volumes
+    monkeypatch.setenv("XN_GRID_LAYOUT", "bricked")
+    vol = ctx.upload_grid(g)
+    p, v = _params_pair(xg, 96, 64)
+    check_parity(ctx, "dda", CAMS[cam], p, v, grid=g, vol=vol, label=f"bricked/{cam}")
+
+
+def test_parity_dda_bricked_non_cubic_and_batched(ctx, monkeypatch):
+    # a grid whose sides are not multiples of the brick; single-frame and
+    # batch renders of the bricked form equal the texture form's
+    import torch
+    import xenodon_gb300 as xg
+    from xenodon_gb300 import volumes
+    g = volumes.ct_shell(37, 21, 50, seed=1, device="cpu")
+    monkeypatch.setenv("XN_GRID_LAYOUT", "bricked")
+    vb = ctx.upload_grid(g)
+    monkeypatch.delenv("XN_GRID_LAYOUT")
+    vt = ctx.upload_grid(g)
+    for cam in ("front", "oblique", "inside", "grazing"):
+        p, v = _params_pair(xg, 61, 47)
+        a, _ = check_parity(ctx, "dda", CAMS[cam], p, v, grid=g, vol=vb, label=f"bricked-ct/{cam}")
+        b, _, _ = ctx.render(vt, "dda", xg.make_camera(*CAMS[cam]), p)
+        assert np.array_equal(a, b)
+    p = xg.make_params(61, 47, 10.0)
+    bufs = [torch.full((47, 61), -1, dtype=torch.int32, device="cuda") for _ in range(2)]
+    jobs = ctx.make_jobs([(vb, "dda", xg.make_camera(*CAMS["oblique"]), p, bufs[0].data_ptr()),
+                          (vt, "dda", xg.make_camera(*CAMS["oblique"]), p, bufs[1].data_ptr())])
+    ctx.render_batch(jobs, 2, xg.BatchConfig(8, 128, 0, 1), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert torch.equal(bufs[0], bufs[1])
+
+
+@pytest.mark.parametrize("ww", ["4", "16", "32"])
+def test_dda_texture_warp_tile_shapes_agree(ctx, blob_volumes, monkeypatch, ww):
+    # XN_DDA_WARP_TILE: warps of 4x8, 16x2 or 32x1 pixels; per-pixel results
+    # and word counts do not depend on the tile shape
+    import xenodon_gb300 as xg
+    g, _, _ = blob_volumes
+    vol = ctx.upload_grid(g)
+    p, v = _params_pair(xg, 93, 58)
+    monkeypatch.setenv("XN_DDA_WARP_TILE", ww)
+    check_parity(ctx, "dda", CAMS["oblique"], p, v, grid=g, vol=vol, label=f"dda-ww{ww}")
+
+
 @pytest.mark.parametrize("cam", ["front", "inside", "grazing"])
 def test_parity_dda_linear_grid_layout(ctx, blob_volumes, monkeypatch, cam):
     # the linear (x-fastest global memory) form of the grid, beside the default texture form

@@ -148,3 +148,92 @@ def test_resident_volumes_are_served_and_never_evicted(ctx, volumes_data):
     # the owner's volume is still usable after the server is gone
     again, _, _ = ctx.render(lean, "esvo", cam, p)
     assert np.array_equal(again, alone)
+
+
+def test_frames_fold_into_the_running_persistent_kernel(ctx, volumes_data):
+    """Requests that arrive while the persistent kernel runs are appended to
+    its ring and rendered by it: with a long idle time one launch takes all of
+    them, each result equal to its render alone."""
+    import time
+    import xenodon_gb300 as xg
+    rng = np.random.default_rng(8)
+    with xg.Server(ctx, fold_idle_us=200000) as server:
+        vols = _register(server, ctx, volumes_data)
+        reqs = _requests(xg, rng, 12)
+        tickets = []
+        for vid, trav, cam, p in reqs:
+            tickets.append(server.submit(vid, trav, xg.make_camera(*cam), p))
+            time.sleep(0.002)
+        for t, req in zip(tickets, reqs):
+            rgba, _ = server.wait(t, timeout=60)
+            assert np.array_equal(rgba, _alone(ctx, vols, req)), req[:2]
+        st = server.stats()
+        assert st["folded"] == 12 + st["republished"]
+        assert st["fold_launches"] == 1
+
+
+def test_persistent_kernel_leaves_when_idle_and_is_launched_again(ctx, volumes_data):
+    import time
+    import xenodon_gb300 as xg
+    rng = np.random.default_rng(9)
+    with xg.Server(ctx, fold_idle_us=100) as server:
+        vols = _register(server, ctx, volumes_data)
+        reqs = _requests(xg, rng, 3)
+        for vid, trav, cam, p in reqs:
+            t = server.submit(vid, trav, xg.make_camera(*cam), p)
+            assert np.array_equal(server.wait(t, timeout=60)[0], _alone(ctx, vols, (vid, trav, cam, p)))
+            time.sleep(0.05)  # far longer than the idle time: the kernel has left
+        assert server.stats()["fold_launches"] == 3
+
+
+def test_full_rings_close_and_alternate(ctx, volumes_data):
+    import xenodon_gb300 as xg
+    rng = np.random.default_rng(10)
+    with xg.Server(ctx, max_batch_jobs=4) as server:
+        vols = _register(server, ctx, volumes_data)
+        reqs = _requests(xg, rng, 30)
+        tickets = [server.submit(vid, trav, xg.make_camera(*cam), p) for vid, trav, cam, p in reqs]
+        for t, req in zip(tickets, reqs):
+            assert np.array_equal(server.wait(t, timeout=60)[0], _alone(ctx, vols, req)), req[:2]
+        st = server.stats()
+        assert st["completed"] == 30 and st["fold_launches"] >= 30 // 4
+
+
+def test_large_frames_take_the_single_frame_path(ctx, volumes_data):
+    """Frames of 2^19 pixels or more run through the single-frame kernels, in
+    bands of rows, on the low-priority stream beside the folded small frames;
+    every result equals its render alone."""
+    import xenodon_gb300 as xg
+    rng = np.random.default_rng(12)
+    with xg.Server(ctx) as server:
+        vols = _register(server, ctx, volumes_data)
+        reqs = _requests(xg, rng, 16)
+        big = [(1, "dda", ((0, 0, -0.8660254), (0, 1, 0), (0.5, 0.5, 2.5)), xg.make_params(1024, 512, 10.0)),
+               (2, "esvo", ((0.35, -0.2, -0.91), (0.0, 0.976, -0.215), (0.2, 0.8, 2.0)),
+                xg.make_params(1280, 720, 10.0)),
+               (4, "svo-rope", ((0.6, 0.3, 0.74), (-0.2, 0.95, 0.0), (0.45, 0.55, 0.5)),
+                xg.make_params(800, 700, 10.0))]
+        mix = reqs[:6] + big[:1] + reqs[6:11] + big[1:] + reqs[11:]
+        tickets = [server.submit(vid, trav, xg.make_camera(*cam), p) for vid, trav, cam, p in mix]
+        for t, req in zip(tickets, mix):
+            assert np.array_equal(server.wait(t, timeout=120)[0], _alone(ctx, vols, req)), req[:2]
+        st = server.stats()
+        assert st["completed"] == len(mix) and st["failed"] == 0
+        assert st["folded"] - st["republished"] == len(reqs)  # the three large frames were not folded
+
+
+def test_server_trace_file(ctx, volumes_data, tmp_path, monkeypatch):
+    """XN_SERVER_TRACE names a file that receives one line per request when
+    the server is destroyed."""
+    import xenodon_gb300 as xg
+    rng = np.random.default_rng(13)
+    path = tmp_path / "trace.txt"
+    monkeypatch.setenv("XN_SERVER_TRACE", str(path))
+    with xg.Server(ctx) as server:
+        _register(server, ctx, volumes_data)
+        reqs = _requests(xg, rng, 5)
+        for t in [server.submit(vid, trav, xg.make_camera(*cam), p) for vid, trav, cam, p in reqs]:
+            server.wait(t, timeout=60)
+    lines = [ln.split() for ln in path.read_text().splitlines() if not ln.startswith("#")]
+    assert len(lines) == 5 and all(len(f) == 8 for f in lines)
+    assert all(float(x) >= 0 for f in lines for x in f[4:])

@@ -81,14 +81,17 @@ class BatchConfig(ctypes.Structure):
 
 
 class ServerConfig(ctypes.Structure):
-    _fields_ = [("hbm_budget", ctypes.c_uint64), ("max_batch_jobs", ctypes.c_int), ("streams", ctypes.c_int)]
+    _fields_ = [("hbm_budget", ctypes.c_uint64), ("max_batch_jobs", ctypes.c_int), ("streams", ctypes.c_int),
+                ("fold_max_pixels", ctypes.c_uint64), ("fold_idle_us", ctypes.c_uint32),
+                ("fold_blocks_per_sm", ctypes.c_uint32)]
 
 
 class ServerStats(ctypes.Structure):
     _fields_ = [("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64), ("batches", ctypes.c_uint64),
                 ("uploads", ctypes.c_uint64), ("evictions", ctypes.c_uint64), ("rays", ctypes.c_uint64),
                 ("hbm_used", ctypes.c_uint64), ("mean_batch", ctypes.c_double), ("p50_ms", ctypes.c_double),
-                ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("mrays_per_s", ctypes.c_double)]
+                ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("mrays_per_s", ctypes.c_double),
+                ("folded", ctypes.c_uint64), ("fold_launches", ctypes.c_uint64), ("republished", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -449,10 +452,14 @@ class BatchGraph:
 class Server:
     """xn_server: continuous batching of render requests on one context."""
 
-    def __init__(self, ctx: Context, hbm_budget: int = 0, max_batch_jobs: int = 256, streams: int = 3):
+    def __init__(self, ctx: Context, hbm_budget: int = 0, max_batch_jobs: int = 1024, streams: int = 2,
+                 fold_max_pixels: int = 0, fold_idle_us: int = 0, fold_blocks_per_sm: int = 0):
+        """max_batch_jobs: job slots of a folding ring; streams: large frames in
+        flight; frames below fold_max_pixels (0: 2^19) fold into the
+        persistent kernel, which leaves after fold_idle_us (0: 300) idle."""
         self.ctx = ctx
         self.lib = ctx.lib
-        cfg = ServerConfig(hbm_budget, max_batch_jobs, streams)
+        cfg = ServerConfig(hbm_budget, max_batch_jobs, streams, fold_max_pixels, fold_idle_us, fold_blocks_per_sm)
         h = ctypes.c_void_p()
         _check(self.lib.xn_server_create(ctx.handle, ctypes.byref(cfg), ctypes.byref(h)))
         self.handle = h

@@ -271,7 +271,8 @@ int upload_grid(xn_ctx* h, const uint8_t* rgba, bool from_device, uint32_t dx, u
     // texture form unless XN_GRID_LAYOUT=linear or the device's 3D texture
     // limits are exceeded
     const char* lay = std::getenv("XN_GRID_LAYOUT");
-    bool use_tex = !(lay && std::strcmp(lay, "linear") == 0);
+    const bool bricked = lay && std::strcmp(lay, "bricked") == 0;
+    bool use_tex = !(lay && (std::strcmp(lay, "linear") == 0 || bricked));
     if (use_tex) {
         cudaDeviceProp prop;
         if (cudaGetDeviceProperties(&prop, c->device) != cudaSuccess || (int)dx > prop.maxTexture3D[0] ||
@@ -314,6 +315,38 @@ int upload_grid(xn_ctx* h, const uint8_t* rgba, bool from_device, uint32_t dx, u
             c->used -= bytes;
             delete v;
             return cuda_fail(e, "xn_volume_upload_grid: texture");
+        }
+        *out = reinterpret_cast<xn_volume*>(v);
+        return XN_OK;
+    }
+    if (bricked) {
+        // the x-fastest grid (the caller's device copy, or a temporary one),
+        // rewritten into bricks
+        if (from_device && (reinterpret_cast<uintptr_t>(rgba) & 3)) {
+            delete v;
+            return fail(XN_ERR_ARG, "xn_volume_upload_grid_device: the grid must be 4-byte aligned");
+        }
+        v->bytes = brick_grid_bytes(dx, dy, dz);
+        v->bricked = 1;
+        if ((r = c->device_alloc(&v->data, v->bytes, "xn_volume_upload_grid: bricks"))) {
+            delete v;
+            return r;
+        }
+        void* src = const_cast<uint8_t*>(rgba);
+        if (!from_device && (r = c->device_alloc(&src, bytes, "xn_volume_upload_grid: staging"))) {
+            c->device_free(v->data, v->bytes);
+            delete v;
+            return r;
+        }
+        e = cudaMemsetAsync(v->data, 0, v->bytes, c->stream);
+        if (e == cudaSuccess && !from_device) e = cudaMemcpyAsync(src, rgba, bytes, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = brick_grid(static_cast<const uint32_t*>(src), dx, dy, dz, v->data, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (!from_device) c->device_free(src, bytes);
+        if (e != cudaSuccess) {
+            c->device_free(v->data, v->bytes);
+            delete v;
+            return cuda_fail(e, "xn_volume_upload_grid: bricks");
         }
         *out = reinterpret_cast<xn_volume*>(v);
         return XN_OK;
@@ -464,6 +497,7 @@ int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_p
         L.grid = v->data;
         L.tex = v->tex;
         L.tex_normalized = v->tex_normalized;
+        L.grid_bricked = v->bricked;
     } else {
         L.nodes = v->data;
         L.layout = v->layout;

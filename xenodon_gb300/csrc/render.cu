@@ -12,6 +12,7 @@
 // it (where the shader would not terminate) raises a bit in the context's
 // error word instead of hanging the GPU.
 #include <cstdint>
+#include <cstdlib>
 #include <cuda_runtime.h>
 
 #include "xn_device.cuh"
@@ -161,6 +162,115 @@ __device__ V3 trace_dda_tex(cudaTextureObject_t tex, uint32_t dx, uint32_t dy, u
         if (side.y == t0) { side.y = side.y + t_delta.y; py += sgn.y; }
         if (side.z == t0) { side.z = side.z + t_delta.z; pz += sgn.z; }
         const V3 next = tex_texel<NORM>(tex, px, py, pz);
+        total = total + tx * (t0 - t);
+        t = t0;
+        tx = next;
+    }
+    return total;
+}
+
+// Bricked form of the grid: 8x8x8-texel bricks (2 KB), x-fastest over a brick
+// grid with one brick of zeros on every side; within a brick, 16-byte groups
+// of 2x2x1 texels ordered (x, y, z pair bits, then the rest) so that a 32-byte
+// sector holds 2x2x2 texels and a 128-byte line 4x4x2.  A ray keeps the group
+// it is in (four texels, one 16-byte load) while its steps stay inside it.
+// The padding makes every read the loop can make -- one cell past the box on
+// a tie, and the fetch one step ahead -- land on zeros, like the texture's
+// border, without a bounds check.
+struct BrickGrid {
+    const uint4* groups;
+    uint32_t dx, dy, dz;
+    uint32_t nbx, nby;  // bricks per row and per column of the padded brick grid
+};
+
+constexpr int BRICK_PAD = 8;  // texels of zeros before the grid on each axis
+
+__host__ __device__ __forceinline__ uint32_t bricks_along(uint32_t d) { return (d + 7) / 8 + 2; }
+
+uint64_t brick_grid_bytes(uint32_t dx, uint32_t dy, uint32_t dz) {
+    return (uint64_t)bricks_along(dx) * bricks_along(dy) * bricks_along(dz) * 2048ull;
+}
+
+// 16-byte group holding padded texel (qx, qy, qz)
+__device__ __forceinline__ uint64_t brick_group(uint32_t nbx, uint32_t nby, uint32_t qx, uint32_t qy, uint32_t qz) {
+    const uint64_t brick = ((uint64_t)(qz >> 3) * nby + (qy >> 3)) * nbx + (qx >> 3);
+    const uint32_t in = ((qx >> 1) & 1) | (((qy >> 1) & 1) << 1) | ((qz & 1) << 2) | (((qx >> 2) & 1) << 3) |
+                        (((qy >> 2) & 1) << 4) | (((qz >> 1) & 3) << 5);
+    return (brick << 7) | in;
+}
+
+__global__ void brick_grid_kernel(const uint32_t* src, uint32_t dx, uint32_t dy, uint32_t dz, uint32_t* dst,
+                                  uint32_t nbx, uint32_t nby) {
+    const uint64_t n = (uint64_t)dx * dy * dz;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t x = (uint32_t)(i % dx);
+        const uint64_t r = i / dx;
+        const uint32_t y = (uint32_t)(r % dy), z = (uint32_t)(r / dy);
+        const uint32_t qx = x + BRICK_PAD, qy = y + BRICK_PAD, qz = z + BRICK_PAD;
+        dst[brick_group(nbx, nby, qx, qy, qz) * 4 + (qx & 1) + 2 * (qy & 1)] = src[i];
+    }
+}
+
+cudaError_t brick_grid(const uint32_t* src, uint32_t dx, uint32_t dy, uint32_t dz, void* bricks, cudaStream_t s) {
+    brick_grid_kernel<<<2048, 256, 0, s>>>(src, dx, dy, dz, static_cast<uint32_t*>(bricks), bricks_along(dx),
+                                           bricks_along(dy));
+    return cudaGetLastError();
+}
+
+// resources/dda.comp:13-53 over the bricked grid; the arithmetic of
+// trace_dda_tex, with the texel taken from the ray's current 16-byte group
+// (loaded again only when a step leaves it) and converted through the
+// shared UNORM8 table.
+template <bool COUNT>
+__device__ V3 trace_dda_brick(const BrickGrid& g, V3 ro, V3 rd, uint32_t& loads, uint32_t& err) {
+    V3 rrd = vs(1.0f) / rd;
+    V3 bias = rrd * ro;
+    V3 box_min = -bias;
+    V3 md = v3((float)g.dx, (float)g.dy, (float)g.dz);
+    V3 box_max = md * rrd - bias;
+    float t_min = max_elem(vmin(box_min, box_max));
+    float t_max = min_elem(vmax(box_min, box_max));
+    if (t_min > t_max) return vs(0.0f);
+    t_min = fmaxf(t_min, 0.0f);
+    ro = ro + rd * t_min;
+    int px = f2i(ro.x), py = f2i(ro.y), pz = f2i(ro.z);
+    V3 t_delta = v3(fabsf(rrd.x), fabsf(rrd.y), fabsf(rrd.z));
+    V3 sgn = v3(gl_sign(rd.x), gl_sign(rd.y), gl_sign(rd.z));
+    const int sx = (int)sgn.x, sy = (int)sgn.y, sz = (int)sgn.z;
+    V3 fr = (v3(floorf(ro.x), floorf(ro.y), floorf(ro.z)) - ro) + vs(0.5f);
+    V3 side = (sgn * fr + vs(0.5f)) * t_delta;
+    float t = 0.0f;
+    V3 total = vs(0.0f);
+    const float lim = t_max - t_min;
+    const uint32_t cap = 2u * (g.dx + g.dy + g.dz) + 64u;
+    uint32_t iter = 0;
+    uint64_t key = ~0ull;
+    uint4 grp = make_uint4(0, 0, 0, 0);
+    auto texel = [&](int x, int y, int z) -> V3 {
+        // the padding covers every cell the loop reaches; the clamp only
+        // guards rays that ran into the iteration cap
+        const uint32_t qx = (uint32_t)min(max(x + BRICK_PAD, 0), (int)g.dx + 2 * BRICK_PAD - 1);
+        const uint32_t qy = (uint32_t)min(max(y + BRICK_PAD, 0), (int)g.dy + 2 * BRICK_PAD - 1);
+        const uint32_t qz = (uint32_t)min(max(z + BRICK_PAD, 0), (int)g.dz + 2 * BRICK_PAD - 1);
+        const uint64_t k = brick_group(g.nbx, g.nby, qx, qy, qz);
+        if (k != key) {
+            grp = __ldg(g.groups + k);
+            key = k;
+        }
+        const uint32_t lo = (qx & 1) ? grp.y : grp.x, hi = (qx & 1) ? grp.w : grp.z;
+        const uint32_t w = (qy & 1) ? hi : lo;
+        return V3{s_unorm_lut[w & 0xFFu], s_unorm_lut[(w >> 8) & 0xFFu], s_unorm_lut[(w >> 16) & 0xFFu]};
+    };
+    V3 tx = texel(px, py, pz);
+    while (t < lim) {
+        if (++iter > cap) { err |= 1u; break; }
+        if (COUNT) ++loads;
+        const float t0 = fminf(side.x, fminf(side.y, side.z));
+        if (side.x == t0) { side.x = side.x + t_delta.x; px += sx; }
+        if (side.y == t0) { side.y = side.y + t_delta.y; py += sy; }
+        if (side.z == t0) { side.z = side.z + t_delta.z; pz += sz; }
+        const V3 next = texel(px, py, pz);
         total = total + tx * (t0 - t);
         t = t0;
         tx = next;
@@ -901,12 +1011,23 @@ __global__ void __launch_bounds__(BLOCK_THREADS) dda_kernel(Frame f, GridVol g, 
     write_outputs(f, o, ix, iy, color, loads, err);
 }
 
-template <bool COUNT, bool NORM>
+// Warps of WW x 32/WW pixels, 2 x 2 warps a block (WW = 8: the 8x4 tiles of
+// every other kernel).
+template <uint32_t WW>
+__device__ __forceinline__ bool pixel_of_thread_ww(const Frame& f, uint32_t& ix, uint32_t& iy) {
+    constexpr uint32_t WH = 32 / WW;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    ix = blockIdx.x * (2 * WW) + (warp & 1u) * WW + lane % WW;
+    iy = blockIdx.y * (2 * WH) + (warp >> 1) * WH + lane / WW;
+    return ix < f.out_w && iy < f.out_h;
+}
+
+template <bool COUNT, bool NORM, uint32_t WW = 8>
 __global__ void __launch_bounds__(BLOCK_THREADS) dda_tex_kernel(Frame f, cudaTextureObject_t tex, uint32_t dx,
                                                                uint32_t dy, uint32_t dz, Outputs o) {
     if (!NORM) fill_unorm_lut();
     uint32_t ix, iy;
-    if (!pixel_of_thread(f, ix, iy)) return;
+    if (!pixel_of_thread_ww<WW>(f, ix, iy)) return;
     uint32_t m = max(dx, max(dy, dz));
     float side = (float)m;
     V3 ro = f.translation * side;
@@ -914,6 +1035,21 @@ __global__ void __launch_bounds__(BLOCK_THREADS) dda_tex_kernel(Frame f, cudaTex
     float ec = __fdiv_rn(voxel_emission_coeff(f, rd), side);
     uint32_t loads = 0, err = 0;
     V3 color = trace_dda_tex<COUNT, NORM>(tex, dx, dy, dz, ro, rd, loads, err) * ec;
+    write_outputs(f, o, ix, iy, color, loads, err);
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(BLOCK_THREADS) dda_brick_kernel(Frame f, BrickGrid g, Outputs o) {
+    fill_unorm_lut();
+    uint32_t ix, iy;
+    if (!pixel_of_thread(f, ix, iy)) return;
+    uint32_t m = max(g.dx, max(g.dy, g.dz));
+    float side = (float)m;
+    V3 ro = f.translation * side;
+    V3 rd = primary_ray(f, ix, iy);
+    float ec = __fdiv_rn(voxel_emission_coeff(f, rd), side);
+    uint32_t loads = 0, err = 0;
+    V3 color = trace_dda_brick<COUNT>(g, ro, rd, loads, err) * ec;
     write_outputs(f, o, ix, iy, color, loads, err);
 }
 
@@ -1298,13 +1434,34 @@ cudaError_t launch_render(const RenderLaunch& L, cudaStream_t stream) {
     if (L.traversal == XN_TRAV_DDA && L.tex) {
         const cudaTextureObject_t t = L.tex;
         const uint32_t x = L.dim[0], y = L.dim[1], z = L.dim[2];
-        if (L.tex_normalized) {
+        // XN_DDA_WARP_TILE = 4 / 16 / 32: warps of 4x8, 16x2 or 32x1 pixels
+        // instead of 8x4 (which texels the lanes of a fetch share depends on it)
+        const char* wt = std::getenv("XN_DDA_WARP_TILE");
+        const uint32_t ww = wt ? (uint32_t)std::atoi(wt) : 8u;
+        if (L.tex_normalized && (ww == 4 || ww == 16 || ww == 32)) {
+            const dim3 g2((L.out_w + 2 * ww - 1) / (2 * ww), (L.out_h + 2 * (32 / ww) - 1) / (2 * (32 / ww)));
+            if (ww == 4) {
+                if (count) dda_tex_kernel<true, true, 4><<<g2, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+                else dda_tex_kernel<false, true, 4><<<g2, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+            } else if (ww == 16) {
+                if (count) dda_tex_kernel<true, true, 16><<<g2, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+                else dda_tex_kernel<false, true, 16><<<g2, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+            } else {
+                if (count) dda_tex_kernel<true, true, 32><<<g2, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+                else dda_tex_kernel<false, true, 32><<<g2, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+            }
+        } else if (L.tex_normalized) {
             if (count) dda_tex_kernel<true, true><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
             else dda_tex_kernel<false, true><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
         } else {
             if (count) dda_tex_kernel<true, false><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
             else dda_tex_kernel<false, false><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
         }
+    } else if (L.traversal == XN_TRAV_DDA && L.grid_bricked) {
+        const BrickGrid g{static_cast<const uint4*>(L.grid), L.dim[0], L.dim[1], L.dim[2], bricks_along(L.dim[0]),
+                          bricks_along(L.dim[1])};
+        if (count) dda_brick_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, g, o);
+        else dda_brick_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, g, o);
     } else if (L.traversal == XN_TRAV_DDA) {
         GridVol g{static_cast<const uchar4*>(L.grid), L.dim[0], L.dim[1], L.dim[2], (uint64_t)L.dim[0],
                   (uint64_t)L.dim[0] * L.dim[1]};
@@ -1382,7 +1539,7 @@ BatchJob make_batch_job(const RenderLaunch& L) {
     j.traversal = L.traversal;
     j.tex = L.tex;
     j.tex_normalized = L.tex_normalized;
-    j.layout = L.traversal == XN_TRAV_DDA ? (L.tex ? 1 : 0) : L.layout;
+    j.layout = L.traversal == XN_TRAV_DDA ? (L.tex ? 1 : L.grid_bricked ? 2 : 0) : L.layout;
     j.grid = L.grid;
     j.nodes = L.nodes;
     j.inner = L.inner;
@@ -1464,6 +1621,10 @@ __device__ __noinline__ uint32_t render_job_pixel(const BatchJob& J, uint32_t ix
             total = J.tex_normalized
                         ? trace_dda_tex<false, true>(J.tex, J.dim[0], J.dim[1], J.dim[2], ro, rd, loads, err)
                         : trace_dda_tex<false, false>(J.tex, J.dim[0], J.dim[1], J.dim[2], ro, rd, loads, err);
+        } else if (J.layout == 2) {
+            const BrickGrid g{static_cast<const uint4*>(J.grid), J.dim[0], J.dim[1], J.dim[2], bricks_along(J.dim[0]),
+                              bricks_along(J.dim[1])};
+            total = trace_dda_brick<false>(g, ro, rd, loads, err);
         } else {
             GridVol g{static_cast<const uchar4*>(J.grid), J.dim[0], J.dim[1], J.dim[2], (uint64_t)J.dim[0],
                       (uint64_t)J.dim[0] * J.dim[1]};
@@ -1687,6 +1848,158 @@ cudaError_t launch_batch(const void* table, unsigned long long* q, uint32_t* err
     case 32: return launch_batch_tw<32>(table, q, err, threads, blocks, chunk, spec, s);
     default: return launch_batch_tw<8>(table, q, err, threads, blocks, chunk, spec, s);
     }
+}
+
+// ------------------------------------------------------------ folding ring ---
+//
+// The persistent kernel of the render server: jobs arrive while it runs.  The
+// host appends a job to a ring in device memory and then raises the published
+// tile count (two copies in one stream, so a count is never visible before the
+// jobs it covers); ring slots not yet written hold tile_begin = ~0, so the
+// binary search over the whole ring finds only published jobs.  A warp claims
+// the next published tile with a compare-and-swap (never past the count),
+// renders it with the batch kernel's per-pixel code, and counts it done; the
+// warp that completes a job raises the job's flag in mapped host memory.
+// Every wait is bounded: a warp that finds nothing to claim sleeps (1 us,
+// doubling to 32 us while nothing comes) and looks again, and once the ring
+// has been idle for idle_ns the whole kernel exits (status bit 0), as it does
+// when the host closes the ring and every published tile is taken.  Jobs
+// published after that are found not done by the host and published again to
+// the next launch; re-rendering a tile writes the same pixels.
+//
+// The polls are relaxed loads and the ring slots are read around L1 (.cg):
+// an acquire load would invalidate the SM's L1 on every poll, which the
+// single-frame kernels running beside this one depend on.  The slot reads
+// depend on the claimed tile number, which depends on the count read, so they
+// are issued after it; the copy of a slot completed before the copy of the
+// count that covers it began.
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// A ring slot copied by the warp into its shared-memory job, read around L1:
+// an L1 line can hold part of a neighbouring slot from before that slot was
+// published.
+__device__ __forceinline__ void load_job_cg(const BatchJob* src, BatchJob* dst, uint32_t lane) {
+    static_assert(sizeof(BatchJob) % 16 == 0 && sizeof(BatchJob) / 16 <= 32, "ring slots are read in 16-byte pieces");
+    const uint4* s = reinterpret_cast<const uint4*>(src);
+    uint4* d = reinterpret_cast<uint4*>(dst);
+    if (lane < sizeof(BatchJob) / 16) d[lane] = __ldcg(s + lane);
+    __syncwarp();
+}
+
+constexpr uint32_t FOLD_THREADS = 128;
+
+template <int TW>
+__global__ void __launch_bounds__(FOLD_THREADS, 4) fold_kernel(FoldCtl* ctl, const BatchJob* ring, uint32_t cap,
+                                                            uint32_t* done_tiles, volatile uint32_t* done_flags,
+                                                            uint32_t* err_word, unsigned long long idle_ns) {
+    fill_unorm_lut();
+    __shared__ BatchJob s_job[FOLD_THREADS / 32];
+    constexpr int TH = 32 / TW;
+    extern __shared__ uint32_t batch_stacks[];
+    SharedStacks stk{batch_stacks + threadIdx.x, batch_stacks + STACK_DEPTH * blockDim.x + threadIdx.x, blockDim.x};
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t err = 0;
+    unsigned long long idle_since = global_ns();
+    uint32_t backoff = 1000;  // ns
+    // every pass claims a tile, sleeps, or exits; the pass count is bounded
+    // as well
+    for (uint32_t pass = 0; pass < (1u << 30); ++pass) {
+        unsigned long long t = ~0ull;
+        int quit = 0;
+        if (lane == 0) {
+            const unsigned long long pub = ld_relaxed_u64(&ctl->published);
+            unsigned long long cur = ld_relaxed_u64(&ctl->taken);
+            while (cur < pub) {
+                const unsigned long long prev = atomicCAS(&ctl->taken, cur, cur + 1);
+                if (prev == cur) {
+                    t = cur;
+                    break;
+                }
+                cur = prev;
+            }
+            if (t == ~0ull) {
+                if (ld_relaxed_u32(&ctl->closed) || ld_relaxed_u32(&ctl->exit_flag)) {
+                    quit = 1;
+                } else if (global_ns() - idle_since > idle_ns) {
+                    atomicExch(&ctl->exit_flag, 1u);
+                    atomicOr(&ctl->status, 1u);
+                    quit = 1;
+                }
+            }
+        }
+        t = __shfl_sync(0xFFFFFFFFu, t, 0);
+        quit = __shfl_sync(0xFFFFFFFFu, quit, 0);
+        if (quit) break;
+        if (t == ~0ull) {
+            __nanosleep(backoff);
+            backoff = backoff < 32000u ? backoff * 2u : 32000u;
+            continue;
+        }
+        backoff = 1000;
+        // the slot of tile t: the last job whose first tile is <= t
+        uint32_t lo = 0, hi = cap;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldcg(&ring[mid].tile_begin) <= t) lo = mid;
+            else hi = mid;
+        }
+        BatchJob& J = s_job[threadIdx.x >> 5];
+        __syncwarp();  // the previous tile's reads of this warp's job are done
+        load_job_cg(ring + lo, &J, lane);
+        const unsigned long long local = t - J.tile_begin;
+        if (local >= (unsigned long long)J.tiles_x * J.tiles_y || !J.rgba) {
+            // cannot happen with the publication order above; the job is left
+            // unfinished (the host renders it again) rather than written astray
+            err |= 4u;
+            idle_since = global_ns();
+            continue;
+        }
+        const uint32_t ty = (uint32_t)(local / J.tiles_x);
+        const uint32_t tx = (uint32_t)(local - (unsigned long long)ty * J.tiles_x);
+        const uint32_t ix = tx * TW + lane % TW, iy = ty * TH + lane / TW;
+        const bool active = ix < J.out_w && iy < J.out_h;
+        const uint32_t px = render_job_pixel_spec<XN_BATCH_ANY>(J, ix, iy, active, err, &stk);
+        if (active) static_cast<uint32_t*>(J.rgba)[(uint64_t)iy * J.out_w + ix] = px;
+        __threadfence();  // this tile's pixels before its count
+        __syncwarp();
+        if (lane == 0) {
+            const uint32_t n = atomicAdd(&done_tiles[lo], 1u) + 1u;
+            if ((unsigned long long)n == (unsigned long long)J.tiles_x * J.tiles_y) {
+                __threadfence_system();
+                done_flags[lo] = 1u;
+            }
+        }
+        idle_since = global_ns();
+    }
+    if (err) atomicOr(err_word, err);
+}
+
+cudaError_t launch_fold(FoldCtl* ctl, const BatchJob* ring, uint32_t cap, uint32_t* done_tiles,
+                        uint32_t* done_flags_mapped, uint32_t* err, uint32_t tile_w, uint32_t blocks,
+                        unsigned long long idle_ns, cudaStream_t s) {
+    const size_t smem = (size_t)2 * STACK_DEPTH * 4 * FOLD_THREADS;
+    if (tile_w == 4)
+        fold_kernel<4><<<blocks, FOLD_THREADS, smem, s>>>(ctl, ring, cap, done_tiles, done_flags_mapped, err, idle_ns);
+    else
+        fold_kernel<8><<<blocks, FOLD_THREADS, smem, s>>>(ctl, ring, cap, done_tiles, done_flags_mapped, err, idle_ns);
+    return cudaGetLastError();
 }
 
 // Resident blocks per SM of the generic kernel with its stacks (the most

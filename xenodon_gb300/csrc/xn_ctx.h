@@ -58,6 +58,7 @@ struct Volume {
     cudaArray_t array = nullptr;
     cudaTextureObject_t tex = 0;
     int tex_normalized = 0;
+    int bricked = 0;  // grid kept in the bricked form (XN_GRID_LAYOUT=bricked)
     uint64_t array_bytes = 0;
     // octree device layout (svo_layout.cu)
     int layout = 0;

@@ -38,6 +38,7 @@ struct RenderLaunch {
     const void* grid;   // uchar4 texels, x fastest (DDA, linear form)
     unsigned long long tex;  // cudaTextureObject_t of the texture form, or 0
     int tex_normalized;      // the texture returns byte/255 itself
+    int grid_bricked;        // `grid` is the bricked form (render.cu BrickGrid), not x-fastest
     uint32_t dim[3];
     const void* nodes;  // reference node words (octree traversals, reference layout)
     int layout;
@@ -61,6 +62,13 @@ struct RenderLaunch {
 };
 
 cudaError_t launch_render(const RenderLaunch& launch, cudaStream_t stream);
+// The bricked grid form (render.cu): 8x8x8-texel bricks of 2 KB, one brick of
+// zeros around the grid on every side; within a brick, 16-byte groups of 2x2x1
+// texels.  Bytes for a dx x dy x dz grid:
+uint64_t brick_grid_bytes(uint32_t dx, uint32_t dy, uint32_t dz);
+// Writes the bricked form of an x-fastest device grid into `bricks`
+// (brick_grid_bytes of zeroed device memory).
+cudaError_t brick_grid(const uint32_t* src, uint32_t dx, uint32_t dy, uint32_t dz, void* bricks, cudaStream_t s);
 
 // One job of a persistent batch launch (device copy of a RenderLaunch plus its
 // place in the batch's tile sequence).
@@ -71,7 +79,7 @@ struct alignas(16) BatchJob {
     uint32_t out_w, out_h;
     int32_t disp_x, disp_y;
     uint32_t disp_w, disp_h;
-    int32_t traversal, layout;  // layout: grids 0 linear / 1 texture; octrees XN_LAYOUT_*
+    int32_t traversal, layout;  // layout: grids 0 linear / 1 texture / 2 bricked; octrees XN_LAYOUT_*
     uint32_t dim[3];
     int32_t tex_normalized;
     int32_t depth_consistent;
@@ -108,5 +116,21 @@ int batch_spec(const BatchJob& j);
 cudaError_t launch_batch(const void* d_table, unsigned long long* d_queue, uint32_t* d_err, uint32_t tile_w,
                          uint32_t threads, uint32_t blocks, uint32_t chunk, int spec, cudaStream_t s);
 int batch_kernel_blocks_per_sm(uint32_t tile_w, uint32_t block_threads);
+
+// Control words of a folding ring (render.cu fold_kernel), in device memory.
+struct alignas(16) FoldCtl {
+    unsigned long long published;  // tiles published (host writes, by copy)
+    unsigned long long taken;      // tiles claimed (device)
+    uint32_t closed;               // host: no more jobs; exit once every published tile is taken
+    uint32_t exit_flag;            // device: the ring went idle; every warp leaves
+    uint32_t status;               // device: bit 0, left because idle
+    uint32_t pad;
+};
+// Launches the persistent folding kernel (128 threads a block, the generic
+// per-pixel form, warp tiles of tile_w x 32/tile_w) over a ring of `cap`
+// job slots; done_flags is mapped host memory (one word per slot).
+cudaError_t launch_fold(FoldCtl* ctl, const BatchJob* ring, uint32_t cap, uint32_t* done_tiles,
+                        uint32_t* done_flags_mapped, uint32_t* err, uint32_t tile_w, uint32_t blocks,
+                        unsigned long long idle_ns, cudaStream_t s);
 
 }  // namespace xn
