@@ -737,13 +737,17 @@ def run_dda_4k_only(args):
     for form in args.dda_4k_forms:  # the grid's form on the device is chosen at upload
         os.environ.pop("XN_GRID_LAYOUT", None)
         os.environ.pop("XN_DDA_WARP_TILE", None)
+        os.environ.pop("XN_DDA_LSU_SHARE", None)
         if form in ("bricked", "linear"):
             os.environ["XN_GRID_LAYOUT"] = form
+        elif form.startswith("hybrid"):  # hybridK: one warp in K reads the x-fastest copy
+            os.environ["XN_GRID_LAYOUT"] = "hybrid"
+            os.environ["XN_DDA_LSU_SHARE"] = form[len("hybrid"):] or "4"
         elif form.startswith("texture-w"):
             os.environ["XN_DDA_WARP_TILE"] = form[len("texture-w"):]
         line[form] = measure_dda_4k(ctx, xg, g, args.dda_4k)
-    os.environ.pop("XN_GRID_LAYOUT", None)
-    os.environ.pop("XN_DDA_WARP_TILE", None)
+    for k in ("XN_GRID_LAYOUT", "XN_DDA_WARP_TILE", "XN_DDA_LSU_SHARE"):
+        os.environ.pop(k, None)
     print(json.dumps(line))
     ctx.close()
     return 0
@@ -919,7 +923,8 @@ def main(argv=None):
     ap.add_argument("--dda-4k", type=int, default=0, metavar="N",
                     help="only the 3840x2160 DDA measurement on an N^3 gas field (for profiling); prints its line")
     ap.add_argument("--dda-4k-forms", nargs="*", default=["texture"],
-                    help="grid forms for --dda-4k: texture, texture-w4/-w16/-w32 (warp tile width), bricked, linear")
+                    help="grid forms for --dda-4k: texture, texture-w4/-w16/-w32 (warp tile width), bricked, linear, "
+                         "hybridK (one warp in K reads an x-fastest copy)")
     ap.add_argument("--svo-4k", type=int, default=0, metavar="N",
                     help="only octree traversals at 3840x2160 on the lean octree of an N^3 gas field (profiling)")
     ap.add_argument("--svo-4k-traversals", nargs="*", default=["esvo"])

@@ -226,6 +226,20 @@ def test_parity_dda_bricked_non_cubic_and_batched(ctx, monkeypatch):
     assert torch.equal(bufs[0], bufs[1])
 
 
+@pytest.mark.parametrize("share", ["1", "2", "4"])
+def test_parity_dda_hybrid_texture_and_lsu_reads(ctx, blob_volumes, monkeypatch, share):
+    # XN_GRID_LAYOUT=hybrid: one warp in XN_DDA_LSU_SHARE reads the x-fastest
+    # copy, the others the texture; every pixel is the reference's either way
+    import xenodon_gb300 as xg
+    g, _, _ = blob_volumes
+    monkeypatch.setenv("XN_GRID_LAYOUT", "hybrid")
+    monkeypatch.setenv("XN_DDA_LSU_SHARE", share)
+    vol = ctx.upload_grid(g)
+    for cam in ("oblique", "grazing"):
+        p, v = _params_pair(xg, 97, 61)
+        check_parity(ctx, "dda", CAMS[cam], p, v, grid=g, vol=vol, label=f"hybrid{share}/{cam}")
+
+
 @pytest.mark.parametrize("ww", ["4", "16", "32"])
 def test_dda_texture_warp_tile_shapes_agree(ctx, blob_volumes, monkeypatch, ww):
     # XN_DDA_WARP_TILE: warps of 4x8, 16x2 or 32x1 pixels; per-pixel results

@@ -272,6 +272,7 @@ int upload_grid(xn_ctx* h, const uint8_t* rgba, bool from_device, uint32_t dx, u
     // limits are exceeded
     const char* lay = std::getenv("XN_GRID_LAYOUT");
     const bool bricked = lay && std::strcmp(lay, "bricked") == 0;
+    const bool hybrid = lay && std::strcmp(lay, "hybrid") == 0;
     bool use_tex = !(lay && (std::strcmp(lay, "linear") == 0 || bricked));
     if (use_tex) {
         cudaDeviceProp prop;
@@ -309,6 +310,24 @@ int upload_grid(xn_ctx* h, const uint8_t* rgba, bool from_device, uint32_t dx, u
             v->tex = make_texture(v->array, norm);
             v->tex_normalized = norm;
             if (!v->tex) e = cudaErrorInvalidValue;
+        }
+        if (e == cudaSuccess && hybrid && v->tex_normalized) {
+            // and the x-fastest copy the hybrid DDA's other warps read
+            if ((r = c->device_alloc(&v->data, bytes, "xn_volume_upload_grid: linear copy"))) {
+                cudaDestroyTextureObject(v->tex);
+                cudaFreeArray(v->array);
+                c->used -= bytes;
+                delete v;
+                return r;
+            }
+            v->bytes = bytes;
+            v->hybrid = 1;
+            e = cudaMemcpyAsync(v->data, rgba, bytes, kind, c->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+            if (e != cudaSuccess) {
+                cudaDestroyTextureObject(v->tex);
+                c->device_free(v->data, v->bytes);
+            }
         }
         if (e != cudaSuccess) {
             cudaFreeArray(v->array);
@@ -498,6 +517,7 @@ int make_launch(const Volume* v, int traversal, const xn_camera* cam, const xn_p
         L.tex = v->tex;
         L.tex_normalized = v->tex_normalized;
         L.grid_bricked = v->bricked;
+        L.grid_hybrid = v->hybrid;
     } else {
         L.nodes = v->data;
         L.layout = v->layout;

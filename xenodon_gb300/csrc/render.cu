@@ -1038,6 +1038,28 @@ __global__ void __launch_bounds__(BLOCK_THREADS) dda_tex_kernel(Frame f, cudaTex
     write_outputs(f, o, ix, iy, color, loads, err);
 }
 
+// The texture unit's data stage limits the texture DDA on large frames (its
+// tex wavefronts near their peak while the L1 banks and the LSU path idle).
+// Here one warp in `share` (warp index % share == 0) reads the x-fastest copy
+// of the grid through the LSU path instead; the arithmetic is the reference's
+// either way, so every pixel is the same.
+template <bool COUNT>
+__global__ void __launch_bounds__(BLOCK_THREADS) dda_hybrid_kernel(Frame f, cudaTextureObject_t tex, GridVol g,
+                                                                  uint32_t share, Outputs o) {
+    uint32_t ix, iy;
+    if (!pixel_of_thread(f, ix, iy)) return;
+    uint32_t m = max(g.dx, max(g.dy, g.dz));
+    float side = (float)m;
+    V3 ro = f.translation * side;
+    V3 rd = primary_ray(f, ix, iy);
+    float ec = __fdiv_rn(voxel_emission_coeff(f, rd), side);
+    uint32_t loads = 0, err = 0;
+    const uint32_t warp = (blockIdx.y * gridDim.x + blockIdx.x) * (BLOCK_THREADS / 32) + (threadIdx.x >> 5);
+    V3 total = warp % share == 0 ? trace_dda<COUNT>(g, ro, rd, loads, err)
+                                 : trace_dda_tex<COUNT, true>(tex, g.dx, g.dy, g.dz, ro, rd, loads, err);
+    write_outputs(f, o, ix, iy, total * ec, loads, err);
+}
+
 template <bool COUNT>
 __global__ void __launch_bounds__(BLOCK_THREADS) dda_brick_kernel(Frame f, BrickGrid g, Outputs o) {
     fill_unorm_lut();
@@ -1438,7 +1460,14 @@ cudaError_t launch_render(const RenderLaunch& L, cudaStream_t stream) {
         // instead of 8x4 (which texels the lanes of a fetch share depends on it)
         const char* wt = std::getenv("XN_DDA_WARP_TILE");
         const uint32_t ww = wt ? (uint32_t)std::atoi(wt) : 8u;
-        if (L.tex_normalized && (ww == 4 || ww == 16 || ww == 32)) {
+        if (L.tex_normalized && L.grid_hybrid) {
+            // XN_DDA_LSU_SHARE: one warp in this many reads the x-fastest copy
+            const char* sh = std::getenv("XN_DDA_LSU_SHARE");
+            const uint32_t share = sh && std::atoi(sh) > 0 ? (uint32_t)std::atoi(sh) : 4u;
+            GridVol g{static_cast<const uchar4*>(L.grid), x, y, z, (uint64_t)x, (uint64_t)x * y};
+            if (count) dda_hybrid_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, g, share, o);
+            else dda_hybrid_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, g, share, o);
+        } else if (L.tex_normalized && (ww == 4 || ww == 16 || ww == 32)) {
             const dim3 g2((L.out_w + 2 * ww - 1) / (2 * ww), (L.out_h + 2 * (32 / ww) - 1) / (2 * (32 / ww)));
             if (ww == 4) {
                 if (count) dda_tex_kernel<true, true, 4><<<g2, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);

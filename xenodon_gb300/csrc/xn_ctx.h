@@ -59,6 +59,7 @@ struct Volume {
     cudaTextureObject_t tex = 0;
     int tex_normalized = 0;
     int bricked = 0;  // grid kept in the bricked form (XN_GRID_LAYOUT=bricked)
+    int hybrid = 0;   // texture plus an x-fastest copy (XN_GRID_LAYOUT=hybrid)
     uint64_t array_bytes = 0;
     // octree device layout (svo_layout.cu)
     int layout = 0;

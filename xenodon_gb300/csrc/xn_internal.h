@@ -39,6 +39,7 @@ struct RenderLaunch {
     unsigned long long tex;  // cudaTextureObject_t of the texture form, or 0
     int tex_normalized;      // the texture returns byte/255 itself
     int grid_bricked;        // `grid` is the bricked form (render.cu BrickGrid), not x-fastest
+    int grid_hybrid;         // both `tex` and an x-fastest `grid`: some warps read each (render.cu)
     uint32_t dim[3];
     const void* nodes;  // reference node words (octree traversals, reference layout)
     int layout;
