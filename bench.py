@@ -524,6 +524,37 @@ def measure_small_dda(ctx, xg, args):
             "max_rgba_diff_vs_oracle": diff}
 
 
+def measure_headless(xg, nodes, side, path):
+    """The `xenodon render --headless` loop on the CT rope octree, esvo at
+    1920x1080, 24 frames of the path written as PNG files: frames per second
+    with the two output sets (frame n+1 renders while frame n is composited
+    and encoded) against XN_HEADLESS_SERIAL=1 (render, wait, save, in turn, as
+    the reference does), and with --discard-output."""
+    import re
+    import tempfile
+    from xenodon_gb300 import cameras
+    result = {"workload": "xenodon render --headless, CT rope octree, esvo, 1920x1080, 24 path frames, PNG output"}
+    with tempfile.TemporaryDirectory() as d:
+        xg.svo_save(Path(d) / "ct.svo", nodes, side)
+        cameras.write_script(Path(d) / "cam.txt", [path[i] for i in range(0, PATH_FRAMES, PATH_FRAMES // 24)][:24])
+        (Path(d) / "h.conf").write_text("device {\n vkindex = 0\n offset = (0, 0)\n extent = (1920, 1080)\n}\n")
+        for mode, extra, env_serial in (("pipelined", ["--output", "f-{}.png"], False),
+                                        ("serial", ["--output", "g-{}.png"], True),
+                                        ("discard", ["--discard-output"], False)):
+            env = dict(os.environ)
+            env.pop("XN_HEADLESS_SERIAL", None)
+            if env_serial:
+                env["XN_HEADLESS_SERIAL"] = "1"
+            p = subprocess.run([str(xg.CLI_PATH), "render", "--headless", "h.conf", "ct.svo", "-s", "esvo", "-e",
+                                str(EMISSION), "--camera", "cam.txt", *extra], cwd=d, env=env, capture_output=True,
+                               text=True, timeout=600)
+            m = re.search(r"frames: (\d+), fps: ([0-9.eE+-]+)", p.stdout)
+            result[mode + "_fps"] = float(m.group(2)) if (p.returncode == 0 and m) else None
+        sizes = [f.stat().st_size for f in Path(d).glob("f-*.png")]
+        result["png_mb_per_frame"] = round(sum(sizes) / max(1, len(sizes)) / 2**20, 2)
+    return result
+
+
 def measure_serving(ctx, xg, args, scene, residents):
     """Continuous batching of the serving mix vs one frame per launch.
 
@@ -872,12 +903,17 @@ def run_ours(args):
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": len(frames) * len(TRAVERSALS),
         "clocks": clk.summary(),
-        "build": {"svo_build_s": round(build_s, 3), "volume_gen_s": round(gen_s, 2)},
+        "build": {"svo_build_s": round(build_s, 3), "volume_gen_s": round(gen_s, 2),
+                  # 4 B per voxel read + 40 B per node written, over the whole call (host grid in,
+                  # host nodes out, copies included)
+                  "algorithmic_gbs": round((4.0 * grid.size / 4 + 40.0 * st["n_nodes"]) / build_s / 1e9, 2),
+                  "voxels_per_s": round(grid.size / 4 / build_s, 1)},
     }
     if rank == 0 and not args.no_extras:
         # the 1024^3 and 2048^3 volumes stay resident for the serving mix
         args.residents = []
-        extras = [("small_dda", lambda: measure_small_dda(ctx, xg, args)),
+        extras = [("headless", lambda: measure_headless(xg, nodes, st["side"], path)),
+                  ("small_dda", lambda: measure_small_dda(ctx, xg, args)),
                   ("batched", lambda: measure_batched(ctx, xg, args))]
         if args.c3_size:
             extras.append(("large", lambda: measure_c3(ctx, xg, args)))

@@ -72,6 +72,21 @@ def test_static_build_single_voxel_grid(ctx):
             assert np.array_equal(nodes, ref)
 
 
+def test_static_build_uniform_grid_is_a_leaf_root(ctx):
+    """A uniform 8^3 grid collapses to a root leaf through the level passes
+    (not the depth-0 case), for every tree type and both heuristics."""
+    grid = np.zeros((8, 8, 8, 4), np.uint8)
+    grid[...] = (90, 10, 200, 255)
+    for svo_type in ("sparse", "dag", "rope"):
+        for heuristic in ("chan-diff", "std-dev"):
+            ref, ref_stats = ctx.build_svo(grid, svo_type, heuristic, 0)
+            assert ref.shape[0] == 1
+            r, nodes, stats, msg = _static_build(grid, svo_type, heuristic, 0, 1)
+            assert r == 0, msg
+            assert stats == ref_stats
+            assert np.array_equal(nodes, ref)
+
+
 def test_static_build_dag_node_buffer_too_small(ctx):
     """A DAG's node count is known only after deduplication; a buffer one
     node short is refused with the count needed."""
