@@ -69,6 +69,21 @@ def load_traffic() -> dict:
     return out
 
 
+def load_issue() -> dict:
+    """Issue-slot and ALU-pipe use per traversal (fractions of peak) from the
+    committed ncu summary, if present: the second bound of the octree
+    traversals, which reread their node words from L1."""
+    p = ROOT / "profiles" / "issue_ct_1080p.txt"
+    out = {}
+    if p.exists():
+        for line in p.read_text().splitlines():
+            f = line.split()
+            if len(f) == 3 and not line.startswith("#"):
+                out[f[0]] = {"issue_active_frac": round(float(f[1]) / 100, 4),
+                             "alu_pipe_frac": round(float(f[2]) / 100, 4)}
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -555,7 +570,7 @@ def measure_headless(xg, nodes, side, path):
     return result
 
 
-def measure_serving(ctx, xg, args, scene, residents):
+def measure_serving(ctx, xg, args, scene, residents, server_kw=None):
     """Continuous batching of the serving mix vs one frame per launch.
 
     Volumes: the 128^3 blob grid and its octree, the CT grid and octree (both
@@ -627,7 +642,7 @@ def measure_serving(ctx, xg, args, scene, residents):
         for arr, dur in zip(arrivals, durations):
             finish = max(finish, arr) + dur
             lat.append((finish - arr) * 1e3)
-        with xg.Server(ctx, hbm_budget=150 << 30) as srv:
+        with xg.Server(ctx, hbm_budget=150 << 30, **(server_kw or {})) as srv:
             for v, (kind, d) in host.items():
                 if kind == "grid":
                     srv.add_grid(v, d)
@@ -713,6 +728,44 @@ def run_svo_4k_only(args):
         line[trav] = measure_svo_4k(ctx, xg, vol, n, trav)
     print(json.dumps(line))
     vol.release()
+    ctx.close()
+    return 0
+
+
+def run_serve_only(args):
+    """--serve-only: the serving mix alone, once per --serve-variants entry
+    (server settings as key=value pairs, e.g. band_pixels=524288,streams=3;
+    an empty entry is the defaults).  Volumes: the CT scene, and with
+    --c3-size the 1024^3 gas field (seed 2, rope octree) and the 2048^3 one
+    (seed 3, lean sparse octree) with their grids, resident on the device."""
+    import torch
+    import xenodon_gb300 as xg
+    from xenodon_gb300 import build as native, volumes
+    native.build()
+    ctx = xg.Context(0)
+    grid, _, _ = make_scene(0)
+    nodes, st = ctx.build_svo(grid, "rope", "chan-diff", 0)
+    residents = []
+    if args.c3_size:
+        for n, seed, lean in ((args.batched_size, 2, False), (args.c3_size, 3, True)):
+            g = volumes.gas_field(n, seed=seed, device="cuda", as_tensor=True)
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()  # the generator's temporaries, before the build's scratch
+            grid_vol = ctx.upload_grid_device(g.data_ptr(), (n, n, n))
+            svo_vol, _ = (ctx.build_svo_volume(g.data_ptr(), (n, n, n), "sparse", lean=True) if lean
+                          else ctx.build_svo_volume(g.data_ptr(), (n, n, n), "rope"))
+            del g
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+            residents.append({"grid": grid_vol, "svo": svo_vol, "dims": (n, n, n), "rope": not lean})
+    out = {}
+    for v in args.serve_variants:
+        kw = {k: int(x) for k, x in (p.split("=") for p in v.split(",") if p)}
+        out[v or "default"] = measure_serving(ctx, xg, args, (grid, nodes, st["side"]), residents, kw)
+    print(json.dumps(out))
+    for r in residents:
+        r["grid"].release()
+        r["svo"].release()
     ctx.close()
     return 0
 
@@ -899,6 +952,11 @@ def run_ours(args):
                      "traffic": traffic, "peak_source": peaks["source"],
                      "algorithmic_bytes_per_launch": int(alg_bytes[dominant])},
         "roofline_per_kernel": per_kernel_roofline,
+        # algorithmic bytes count every reference word a ray reads; the
+        # octree walks reread their words from L1, so their fractions are
+        # not DRAM use (svo-naive, restarting from the root, is above 1) and
+        # issue slots bound them: the figures of the ncu capture
+        "issue": {"source": "ncu, profiles/issue_ct_1080p.txt", "per_kernel": load_issue()},
         "e2e": {"value": round(e2e, 2), "unit": "Mrays/s", "h2d_bytes_per_step": len(TRAVERSALS) * cam_bytes,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": len(frames) * len(TRAVERSALS),
@@ -947,8 +1005,9 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--band-rows", type=int, default=64, help="rows per oracle call of the CPU legs")
-    ap.add_argument("--cpu-bands", type=int, default=4, help="bands per frame and traversal of cpu_baseline")
-    ap.add_argument("--cpu-frames", type=int, default=2, help="frames of cpu_baseline")
+    ap.add_argument("--cpu-bands", type=int, default=16, help="bands per frame and traversal of cpu_baseline")
+    ap.add_argument("--cpu-frames", type=int, default=6,
+                    help="frames of cpu_baseline (with 16 bands: about 10 s on 16 cores)")
     ap.add_argument("--single-core-rows", type=int, default=8, help="rows of the single-core cpu_baseline band")
     ap.add_argument("--ref-bands", type=int, default=3, help="bands per frame and traversal of --impl reference")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -969,6 +1028,9 @@ def main(argv=None):
     ap.add_argument("--c3-frames", type=int, default=16)
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 200.0, 1000.0, 2000.0, 0.0])
+    ap.add_argument("--serve-only", action="store_true", help="the serving mix alone, per --serve-variants")
+    ap.add_argument("--serve-variants", nargs="*", default=[""],
+                    help="server settings per run, key=value[,key=value] (Server keyword arguments)")
     args = ap.parse_args(argv)
     if args.impl == "reference":
         return run_reference(args)
@@ -978,6 +1040,8 @@ def main(argv=None):
         return run_svo_4k_only(args)
     if args.batch_only:
         return run_batch_only(args)
+    if args.serve_only:
+        return run_serve_only(args)
     return run_ours(args)
 
 

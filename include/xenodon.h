@@ -266,17 +266,18 @@ XN_API int xn_batch_graph_destroy(xn_batch_graph* g);
  * high-priority stream, and copied out as soon as its own tiles are done.
  * The kernel leaves after fold_idle_us without work (its waits are bounded)
  * and is launched again when frames arrive.  Larger frames (each fills the GPU
- * alone) run through the single-frame kernels on a low-priority stream, in
- * bands of rows, `streams` of them in flight.  A copy thread moves finished
- * frames into the callers' buffers. */
+ * alone) run through the single-frame kernels on low-priority streams,
+ * `streams` of them in flight, whole or in bands of rows.  A copy thread
+ * moves finished frames into the callers' buffers. */
 typedef struct xn_server xn_server;
 typedef struct {
     uint64_t hbm_budget;   /* bytes for resident volumes and in-flight frames; 0 = the context's budget */
     int max_batch_jobs;    /* job slots of a folding ring: frames one persistent launch takes (default 1024) */
-    int streams;           /* large frames in flight at once (default 2) */
+    int streams;           /* large frames in flight at once, one stream each (default 2, at most 16) */
     uint64_t fold_max_pixels;    /* frames below this many pixels are folded (0: 2^19) */
     uint32_t fold_idle_us;       /* the persistent kernel leaves after this long without work (0: 300) */
     uint32_t fold_blocks_per_sm; /* its warps per SM in units of 8 (blocks of 128 threads), 1 or 2 (0: 1) */
+    uint64_t band_pixels;  /* large frames are launched in bands of rows of about this many pixels (0: whole) */
 } xn_server_config;
 typedef struct {
     uint64_t completed, failed, batches, uploads, evictions, rays, hbm_used;

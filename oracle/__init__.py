@@ -56,11 +56,12 @@ def build() -> None:
 
 
 def build_ref() -> bool:
-    """Compile the reference's own builder when the reference checkout exists."""
-    ref = subprocess.run(["make", "-s", "-C", str(HERE), "--no-print-directory", "print-reference"],
-                         capture_output=True, text=True).stdout.strip()
+    """Compile the reference's own builder from the checkout that
+    XENODON_REFERENCE names; without one, report whether a builder was
+    compiled before."""
+    ref = os.environ.get("XENODON_REFERENCE", "")
     if not ref or not (Path(ref) / "src" / "model" / "OctreeConstruction.h").exists():
-        return False
+        return REF_BUILDER.exists()
     subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REFERENCE={ref}"], check=True)
     return True
 

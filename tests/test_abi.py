@@ -104,3 +104,33 @@ def test_null_arguments_are_rejected(built_library):
     out = ctypes.POINTER(ctypes.c_uint32)()
     st = xg.BuildStats()
     assert lib.xn_build_svo(None, None, 1, 1, 1, 0, 0, 0.0, ctypes.byref(out), ctypes.byref(st)) == xg.XN_ERR_ARG
+
+
+# ctypes mirror -> the header's typedef name
+MIRRORS = {"Camera": "xn_camera", "Rect": "xn_rect", "Params": "xn_params", "VolumeInfo": "xn_volume_info",
+           "Job": "xn_job", "BatchConfig": "xn_batch_config", "ServerConfig": "xn_server_config",
+           "ServerStats": "xn_server_metrics", "BuildStats": "xn_build_stats"}
+
+
+def test_ctypes_structures_match_the_header(tmp_path):
+    """Size and every field offset of the Python mirrors equal the C
+    compiler's for include/xenodon.h (a field added on one side only would
+    shift what the library reads)."""
+    import ctypes
+    import xenodon_gb300 as xg
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "xenodon.h"', "int main(void) {"]
+    expect = []
+    for py, c in MIRRORS.items():
+        cls = getattr(xg, py)
+        lines.append(f'printf("{c} %zu\\n", sizeof({c}));')
+        expect.append(f"{c} {ctypes.sizeof(cls)}")
+        for name, _ in cls._fields_:
+            lines.append(f'printf("{c}.{name} %zu\\n", offsetof({c}, {name}));')
+            expect.append(f"{c}.{name} {getattr(cls, name).offset}")
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    assert [g for g in got if g] == expect

@@ -199,13 +199,15 @@ def test_full_rings_close_and_alternate(ctx, volumes_data):
         assert st["completed"] == 30 and st["fold_launches"] >= 30 // 4
 
 
-def test_large_frames_take_the_single_frame_path(ctx, volumes_data):
-    """Frames of 2^19 pixels or more run through the single-frame kernels, in
-    bands of rows, on the low-priority stream beside the folded small frames;
+@pytest.mark.parametrize("band_pixels,streams", [(0, 2), (1 << 16, 2), (100000, 1), (0, 3)])
+def test_large_frames_take_the_single_frame_path(ctx, volumes_data, band_pixels, streams):
+    """Frames of 2^19 pixels or more run through the single-frame kernels on
+    low-priority streams beside the folded small frames, whole or in bands of
+    rows (a band of 100000 pixels does not divide the frames' rows evenly);
     every result equals its render alone."""
     import xenodon_gb300 as xg
     rng = np.random.default_rng(12)
-    with xg.Server(ctx) as server:
+    with xg.Server(ctx, band_pixels=band_pixels, streams=streams) as server:
         vols = _register(server, ctx, volumes_data)
         reqs = _requests(xg, rng, 16)
         big = [(1, "dda", ((0, 0, -0.8660254), (0, 1, 0), (0.5, 0.5, 2.5)), xg.make_params(1024, 512, 10.0)),

@@ -83,7 +83,7 @@ class BatchConfig(ctypes.Structure):
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget", ctypes.c_uint64), ("max_batch_jobs", ctypes.c_int), ("streams", ctypes.c_int),
                 ("fold_max_pixels", ctypes.c_uint64), ("fold_idle_us", ctypes.c_uint32),
-                ("fold_blocks_per_sm", ctypes.c_uint32)]
+                ("fold_blocks_per_sm", ctypes.c_uint32), ("band_pixels", ctypes.c_uint64)]
 
 
 class ServerStats(ctypes.Structure):
@@ -453,13 +453,17 @@ class Server:
     """xn_server: continuous batching of render requests on one context."""
 
     def __init__(self, ctx: Context, hbm_budget: int = 0, max_batch_jobs: int = 1024, streams: int = 2,
-                 fold_max_pixels: int = 0, fold_idle_us: int = 0, fold_blocks_per_sm: int = 0):
+                 fold_max_pixels: int = 0, fold_idle_us: int = 0, fold_blocks_per_sm: int = 0,
+                 band_pixels: int = 0):
         """max_batch_jobs: job slots of a folding ring; streams: large frames in
         flight; frames below fold_max_pixels (0: 2^19) fold into the
-        persistent kernel, which leaves after fold_idle_us (0: 300) idle."""
+        persistent kernel, which leaves after fold_idle_us (0: 300) idle;
+        band_pixels: large frames in bands of rows of about that many pixels
+        (0: one launch per frame)."""
         self.ctx = ctx
         self.lib = ctx.lib
-        cfg = ServerConfig(hbm_budget, max_batch_jobs, streams, fold_max_pixels, fold_idle_us, fold_blocks_per_sm)
+        cfg = ServerConfig(hbm_budget, max_batch_jobs, streams, fold_max_pixels, fold_idle_us, fold_blocks_per_sm,
+                           band_pixels)
         h = ctypes.c_void_p()
         _check(self.lib.xn_server_create(ctx.handle, ctypes.byref(cfg), ctypes.byref(h)))
         self.handle = h

@@ -15,15 +15,19 @@
 //    whose slots are used up is closed while the other ring takes new jobs;
 //    jobs that reached a ring after its kernel left are published again;
 //  - large frames (each fills the GPU alone) run through the single-frame
-//    kernels on a low-priority stream, in bands of rows, a few frames in
-//    flight, each copied out as soon as it is done.
+//    kernels, each on one of `streams` low-priority streams (a few frames in
+//    flight, so one frame's last blocks overlap the next frame's first), and
+//    are copied out on that stream as soon as they are done.
 //
-// The persistent kernel's blocks, on the high-priority stream, are placed
-// ahead of the next band's blocks whenever a band ends, so a small frame
-// waits at most for one band of a large frame.  Output buffers come from a
-// pool, so admission does not allocate; a copy thread moves finished frames
-// from pinned staging into the callers' buffers.  Latency is measured from
-// submit to the frame in the caller's buffer.
+// The persistent kernel runs on a high-priority stream: the block scheduler
+// places its blocks ahead of the pending blocks of the large frames' grids
+// as those retire, so a small frame does not wait for a large frame to end.
+// A large frame can also be launched in bands of rows (band_pixels), which
+// bounds how long a newly launched persistent kernel waits to be placed.
+// Output buffers come from a pool, so admission does not allocate; a copy
+// thread moves finished frames from pinned staging into the callers'
+// buffers.  Latency is measured from submit to the frame in the caller's
+// buffer.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -167,7 +171,9 @@ struct xn_server {
     std::vector<Request*> copying;    // D2H copies in flight (an event each)
     std::deque<Request*> copy_queue;  // copied to staging; the copy thread finishes them
     std::vector<Request*> large_inflight;
-    cudaStream_t fold_stream = nullptr, ctl_stream = nullptr, copy_stream = nullptr, large_stream = nullptr;
+    cudaStream_t fold_stream = nullptr, ctl_stream = nullptr, copy_stream = nullptr;
+    std::vector<cudaStream_t> large_streams;  // low priority, one per large frame in flight
+    size_t next_large = 0;
     FoldRing rings[FOLD_RINGS];
     int cur_ring = 0;
     Pool dev_pool, host_pool;
@@ -390,7 +396,7 @@ bool xn_server::poll_copies() {
         copying[i] = copying.back();
         copying.pop_back();
         q->t_copied = Clock::now();
-        if (q->large) q->t_flagged = q->t_copied;  // kernel and copy share the large stream
+        if (q->large) q->t_flagged = q->t_copied;  // kernel and copy share the frame's stream
         event_pool.push_back(q->copied);
         q->copied = nullptr;
         unadmit(q);
@@ -516,15 +522,17 @@ void xn_server::launch_large() {
         // at most one band, not a whole large frame (the pixels are the same:
         // every band keeps the frame's display region)
         const xn_rect o = q->params.output_region;
-        const uint32_t band = (uint32_t)std::max<uint64_t>(1, cfg.fold_max_pixels / o.width);
+        const uint32_t band =
+            cfg.band_pixels ? (uint32_t)std::max<uint64_t>(1, cfg.band_pixels / o.width) : o.height;
+        cudaStream_t st = large_streams[next_large];
+        next_large = (next_large + 1) % large_streams.size();
         int r = XN_OK;
         for (uint32_t y0 = 0; y0 < o.height && !r; y0 += band) {
             xn_params p = q->params;
             p.output_region.y = o.y + (int32_t)y0;
             p.output_region.height = std::min(band, o.height - y0);
             r = xn_render_device(ctx, volumes[q->volume_id].dev, q->traversal, &q->cam, &p,
-                                 static_cast<uint8_t*>(q->d_out) + (uint64_t)y0 * o.width * 4, nullptr, nullptr,
-                                 large_stream);
+                                 static_cast<uint8_t*>(q->d_out) + (uint64_t)y0 * o.width * 4, nullptr, nullptr, st);
         }
         if (r) {
             unadmit(q);
@@ -534,7 +542,7 @@ void xn_server::launch_large() {
         ++launches;
         ++launched_jobs;
         q->t_launch = Clock::now();
-        start_copy(q, large_stream);
+        start_copy(q, st);
         if (q->status == 1) large_inflight.push_back(q);
     }
 }
@@ -628,6 +636,7 @@ XN_API int xn_server_create(xn_ctx* ctx, const xn_server_config* cfg, xn_server*
     if (s->cfg.max_batch_jobs <= 0) s->cfg.max_batch_jobs = 1024;
     if (s->cfg.max_batch_jobs > (1 << 16)) s->cfg.max_batch_jobs = 1 << 16;
     if (s->cfg.streams <= 0) s->cfg.streams = 2;
+    if (s->cfg.streams > 16) s->cfg.streams = 16;
     if (s->cfg.fold_max_pixels == 0) s->cfg.fold_max_pixels = 1ull << 19;
     if (s->cfg.fold_idle_us == 0) s->cfg.fold_idle_us = 300;
     if (s->cfg.fold_blocks_per_sm == 0) s->cfg.fold_blocks_per_sm = 1;
@@ -644,9 +653,13 @@ XN_API int xn_server_create(xn_ctx* ctx, const xn_server_config* cfg, xn_server*
     int lo = 0, hi = 0;  // numerically lower is more urgent
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
     bool ok = cudaStreamCreateWithPriority(&s->fold_stream, cudaStreamNonBlocking, hi) == cudaSuccess &&
-              cudaStreamCreateWithPriority(&s->large_stream, cudaStreamNonBlocking, lo) == cudaSuccess &&
               cudaStreamCreateWithFlags(&s->ctl_stream, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithPriority(&s->copy_stream, cudaStreamNonBlocking, hi) == cudaSuccess;
+    for (int i = 0; ok && i < s->cfg.streams; ++i) {
+        cudaStream_t st = nullptr;
+        ok = cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, lo) == cudaSuccess;
+        if (ok) s->large_streams.push_back(st);
+    }
     const uint64_t cap = (uint64_t)s->cfg.max_batch_jobs;
     for (auto& r : s->rings) {
         if (!ok) break;
@@ -701,8 +714,9 @@ XN_API int xn_server_destroy(xn_server* s) {
     if (s->copier.joinable()) s->copier.join();
     s->cv_done.notify_all();
     cudaSetDevice(s->c->device);
-    for (cudaStream_t st : {s->fold_stream, s->ctl_stream, s->copy_stream, s->large_stream})
+    for (cudaStream_t st : {s->fold_stream, s->ctl_stream, s->copy_stream})
         if (st) cudaStreamSynchronize(st);
+    for (cudaStream_t st : s->large_streams) cudaStreamSynchronize(st);
     for (auto& kv : s->volumes)
         if (kv.second.dev && !kv.second.external) xn_volume_release(kv.second.dev);
     for (auto& r : s->rings) {
@@ -719,8 +733,9 @@ XN_API int xn_server_destroy(xn_server* s) {
     s->dev_pool.release();
     s->host_pool.release();
     for (cudaEvent_t e : s->event_pool) cudaEventDestroy(e);
-    for (cudaStream_t st : {s->fold_stream, s->ctl_stream, s->copy_stream, s->large_stream})
+    for (cudaStream_t st : {s->fold_stream, s->ctl_stream, s->copy_stream})
         if (st) cudaStreamDestroy(st);
+    for (cudaStream_t st : s->large_streams) cudaStreamDestroy(st);
     for (auto& kv : s->requests) delete kv.second;
     if (!s->trace_path.empty()) {
         if (std::FILE* f = std::fopen(s->trace_path.c_str(), "a")) {
