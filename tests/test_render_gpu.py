@@ -423,16 +423,28 @@ def test_df_lane_walk_equals_warp_walk(ctx, monkeypatch, n, cam):
     assert np.array_equal(em_1, em_w) and np.array_equal(loads_1, loads_w)
 
 
+@pytest.mark.parametrize("read", ["raw", "packed"])
 @pytest.mark.parametrize("cam", ["front", "inside", "grazing"])
-def test_dda_raw_texel_reads_equal_normalized(ctx, blob_volumes, monkeypatch, cam):
+def test_dda_raw_texel_reads_equal_normalized(ctx, blob_volumes, monkeypatch, cam, read):
     # XN_TEX_READ=raw: the texture returns the bytes and the kernel converts
-    # them through its shared table; same bits as the texture unit's UNORM read
+    # them through its shared table; packed: one 32-bit word per fetch,
+    # converted in registers; same bits as the texture unit's UNORM read,
+    # single-frame and batched
     import xenodon_gb300 as xg
+    import torch
     g, _, _ = blob_volumes
     p, v = _params_pair(xg, 77, 53)
     norm_vol = ctx.upload_grid(g)
     a, _ = check_parity(ctx, "dda", CAMS[cam], p, v, grid=g, vol=norm_vol, label=f"dda-norm/{cam}")
-    monkeypatch.setenv("XN_TEX_READ", "raw")
+    monkeypatch.setenv("XN_TEX_READ", read)
     raw_vol = ctx.upload_grid(g)
-    b, _ = check_parity(ctx, "dda", CAMS[cam], p, v, grid=g, vol=raw_vol, label=f"dda-raw/{cam}")
+    b, _ = check_parity(ctx, "dda", CAMS[cam], p, v, grid=g, vol=raw_vol, label=f"dda-{read}/{cam}")
     assert np.array_equal(a, b)
+    out = torch.empty((p.output_region.height, p.output_region.width), dtype=torch.int32, device="cuda")
+    jobs = ctx.make_jobs([(raw_vol, "dda", xg.make_camera(*CAMS[cam]), p, out.data_ptr())])
+    sptr = torch.cuda.current_stream().cuda_stream
+    ctx.render_batch(jobs, 1, xg.BatchConfig(8, 128, 0, 1), sptr)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy().view(np.uint8).reshape(a.shape), a)
+    raw_vol.release()
+    norm_vol.release()

@@ -150,12 +150,15 @@ def test_resident_volumes_are_served_and_never_evicted(ctx, volumes_data):
     assert np.array_equal(again, alone)
 
 
-def test_frames_fold_into_the_running_persistent_kernel(ctx, volumes_data):
+@pytest.mark.parametrize("threads", ["128", "32"])
+def test_frames_fold_into_the_running_persistent_kernel(ctx, volumes_data, monkeypatch, threads):
     """Requests that arrive while the persistent kernel runs are appended to
     its ring and rendered by it: with a long idle time one launch takes all of
-    them, each result equal to its render alone."""
+    them, each result equal to its render alone (blocks of 128 threads or of
+    one warp, XN_FOLD_THREADS)."""
     import time
     import xenodon_gb300 as xg
+    monkeypatch.setenv("XN_FOLD_THREADS", threads)
     rng = np.random.default_rng(8)
     with xg.Server(ctx, fold_idle_us=200000) as server:
         vols = _register(server, ctx, volumes_data)
@@ -239,3 +242,31 @@ def test_server_trace_file(ctx, volumes_data, tmp_path, monkeypatch):
     lines = [ln.split() for ln in path.read_text().splitlines() if not ln.startswith("#")]
     assert len(lines) == 5 and all(len(f) == 8 for f in lines)
     assert all(float(x) >= 0 for f in lines for x in f[4:])
+
+
+def test_arrivals_across_idle_exits_are_all_rendered(ctx, volumes_data):
+    """With an idle time shorter than the gaps between arrivals the persistent
+    kernel leaves and is launched again many times while frames keep coming;
+    a kernel that has decided to leave takes no new tiles, so frames
+    published to it meanwhile go to the next launch.  Every frame is
+    rendered, equal to its render alone, and none waits for long."""
+    import time
+    import xenodon_gb300 as xg
+    rng = np.random.default_rng(14)
+    with xg.Server(ctx, fold_idle_us=50) as server:
+        vols = _register(server, ctx, volumes_data)
+        reqs = _requests(xg, rng, 60)
+        tickets = []
+        t0 = time.perf_counter()
+        for vid, trav, cam, p in reqs:
+            tickets.append(server.submit(vid, trav, xg.make_camera(*cam), p))
+            time.sleep(float(rng.uniform(0.0, 0.0005)))
+        for t, req in zip(tickets, reqs):
+            rgba, lat = server.wait(t, timeout=60)
+            assert np.array_equal(rgba, _alone(ctx, vols, req)), req[:2]
+            assert lat < 5000.0
+        assert time.perf_counter() - t0 < 60.0
+        st = server.stats()
+        assert st["completed"] == 60 and st["failed"] == 0
+        assert st["folded"] == 60 + st["republished"]
+        assert st["fold_launches"] >= 2

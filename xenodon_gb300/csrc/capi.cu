@@ -283,15 +283,18 @@ int upload_grid(xn_ctx* h, const uint8_t* rgba, bool from_device, uint32_t dx, u
     cudaError_t e = cudaSuccess;
     if (use_tex) {
         // the texture unit converts to float when it gives byte/255 exactly,
-        // unless XN_TEX_READ=raw (4-byte texels, converted in the kernel)
+        // unless XN_TEX_READ=raw (four bytes per fetch, converted in the
+        // kernel) or packed (one 32-bit word per fetch, converted in the
+        // kernel)
         const char* rd = std::getenv("XN_TEX_READ");
-        const bool norm = !(rd && std::strcmp(rd, "raw") == 0) && texture_unorm_exact(c) == 1;
+        const bool packed = rd && std::strcmp(rd, "packed") == 0;
+        const bool norm = !packed && !(rd && std::strcmp(rd, "raw") == 0) && texture_unorm_exact(c) == 1;
         if (c->budget && c->used.load() + bytes > c->budget) {
             delete v;
             return fail(XN_ERR_BUDGET, "xn_volume_upload_grid: %llu bytes exceed the HBM budget",
                         (unsigned long long)bytes);
         }
-        cudaChannelFormatDesc d = cudaCreateChannelDesc<uchar4>();
+        cudaChannelFormatDesc d = packed ? cudaCreateChannelDesc<unsigned int>() : cudaCreateChannelDesc<uchar4>();
         e = cudaMalloc3DArray(&v->array, &d, make_cudaExtent(dx, dy, dz));
         if (e != cudaSuccess) {
             delete v;
@@ -308,10 +311,10 @@ int upload_grid(xn_ctx* h, const uint8_t* rgba, bool from_device, uint32_t dx, u
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         if (e == cudaSuccess) {
             v->tex = make_texture(v->array, norm);
-            v->tex_normalized = norm;
+            v->tex_normalized = packed ? 2 : norm ? 1 : 0;
             if (!v->tex) e = cudaErrorInvalidValue;
         }
-        if (e == cudaSuccess && hybrid && v->tex_normalized) {
+        if (e == cudaSuccess && hybrid && v->tex_normalized == 1) {
             // and the x-fastest copy the hybrid DDA's other warps read
             if ((r = c->device_alloc(&v->data, bytes, "xn_volume_upload_grid: linear copy"))) {
                 cudaDestroyTextureObject(v->tex);

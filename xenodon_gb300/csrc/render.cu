@@ -111,20 +111,26 @@ __device__ __forceinline__ V3 leaf_rgb(uint32_t col) {
     return V3{s_unorm_lut[col & 0xFFu], s_unorm_lut[(col >> 8) & 0xFFu], s_unorm_lut[(col >> 16) & 0xFFu]};
 }
 
-template <bool NORM>
+// Texel reads of the three texture forms (TEX_*): the texture unit returns
+// byte/255 as four floats; or four bytes, converted through the shared
+// table (the kernel fills it); or one 32-bit word of four bytes (a
+// one-channel texture over the same bytes: one register returned per lane
+// instead of four), converted in registers.
+constexpr int TEX_RAW = 0, TEX_NORM = 1, TEX_PACKED = 2;
+template <int MODE>
 __device__ __forceinline__ V3 tex_texel(cudaTextureObject_t t, float x, float y, float z) {
-    if (NORM) {
+    if (MODE == TEX_NORM) {
         float4 v = tex3D<float4>(t, x, y, z);
         return V3{v.x, v.y, v.z};
     }
-    // raw bytes, converted through the shared table (the kernel fills it)
+    if (MODE == TEX_PACKED) return unpack_rgb_bits(tex3D<unsigned int>(t, x, y, z));
     uchar4 v = tex3D<uchar4>(t, x, y, z);
     return V3{s_unorm_lut[v.x], s_unorm_lut[v.y], s_unorm_lut[v.z]};
 }
 
 // resources/dda.comp:13-53 over the texture form; coordinates are kept as
 // texel centres (integers + 0.5, exact in float).
-template <bool COUNT, bool NORM>
+template <bool COUNT, int NORM>
 __device__ V3 trace_dda_tex(cudaTextureObject_t tex, uint32_t dx, uint32_t dy, uint32_t dz, V3 ro, V3 rd,
                             uint32_t& loads, uint32_t& err) {
     V3 rrd = vs(1.0f) / rd;
@@ -1022,10 +1028,10 @@ __device__ __forceinline__ bool pixel_of_thread_ww(const Frame& f, uint32_t& ix,
     return ix < f.out_w && iy < f.out_h;
 }
 
-template <bool COUNT, bool NORM, uint32_t WW = 8>
+template <bool COUNT, int NORM, uint32_t WW = 8>
 __global__ void __launch_bounds__(BLOCK_THREADS) dda_tex_kernel(Frame f, cudaTextureObject_t tex, uint32_t dx,
                                                                uint32_t dy, uint32_t dz, Outputs o) {
-    if (!NORM) fill_unorm_lut();
+    if (NORM == TEX_RAW) fill_unorm_lut();
     uint32_t ix, iy;
     if (!pixel_of_thread_ww<WW>(f, ix, iy)) return;
     uint32_t m = max(dx, max(dy, dz));
@@ -1460,14 +1466,14 @@ cudaError_t launch_render(const RenderLaunch& L, cudaStream_t stream) {
         // instead of 8x4 (which texels the lanes of a fetch share depends on it)
         const char* wt = std::getenv("XN_DDA_WARP_TILE");
         const uint32_t ww = wt ? (uint32_t)std::atoi(wt) : 8u;
-        if (L.tex_normalized && L.grid_hybrid) {
+        if (L.tex_normalized == TEX_NORM && L.grid_hybrid) {
             // XN_DDA_LSU_SHARE: one warp in this many reads the x-fastest copy
             const char* sh = std::getenv("XN_DDA_LSU_SHARE");
             const uint32_t share = sh && std::atoi(sh) > 0 ? (uint32_t)std::atoi(sh) : 4u;
             GridVol g{static_cast<const uchar4*>(L.grid), x, y, z, (uint64_t)x, (uint64_t)x * y};
             if (count) dda_hybrid_kernel<true><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, g, share, o);
             else dda_hybrid_kernel<false><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, g, share, o);
-        } else if (L.tex_normalized && (ww == 4 || ww == 16 || ww == 32)) {
+        } else if (L.tex_normalized == TEX_NORM && (ww == 4 || ww == 16 || ww == 32)) {
             const dim3 g2((L.out_w + 2 * ww - 1) / (2 * ww), (L.out_h + 2 * (32 / ww) - 1) / (2 * (32 / ww)));
             if (ww == 4) {
                 if (count) dda_tex_kernel<true, true, 4><<<g2, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
@@ -1479,9 +1485,12 @@ cudaError_t launch_render(const RenderLaunch& L, cudaStream_t stream) {
                 if (count) dda_tex_kernel<true, true, 32><<<g2, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
                 else dda_tex_kernel<false, true, 32><<<g2, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
             }
-        } else if (L.tex_normalized) {
-            if (count) dda_tex_kernel<true, true><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
-            else dda_tex_kernel<false, true><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+        } else if (L.tex_normalized == TEX_NORM) {
+            if (count) dda_tex_kernel<true, TEX_NORM><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+            else dda_tex_kernel<false, TEX_NORM><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+        } else if (L.tex_normalized == TEX_PACKED) {
+            if (count) dda_tex_kernel<true, TEX_PACKED><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
+            else dda_tex_kernel<false, TEX_PACKED><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
         } else {
             if (count) dda_tex_kernel<true, false><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
             else dda_tex_kernel<false, false><<<grid, BLOCK_THREADS, 0, stream>>>(f, t, x, y, z, o);
@@ -1585,7 +1594,8 @@ BatchJob make_batch_job(const RenderLaunch& L) {
 
 int batch_spec(const BatchJob& j) {
     if (j.traversal == XN_TRAV_DDA)
-        return j.layout == 1 ? (j.tex_normalized ? XN_BATCH_DDA_TEX_NORM : XN_BATCH_DDA_TEX_RAW) : XN_BATCH_ANY;
+        return j.layout == 1 ? (j.tex_normalized == TEX_NORM ? XN_BATCH_DDA_TEX_NORM : XN_BATCH_DDA_TEX_RAW)
+                             : XN_BATCH_ANY;
     if (j.layout != XN_LAYOUT_COMPACT) return XN_BATCH_ANY;
     switch (j.traversal) {
     case XN_TRAV_ESVO: return XN_BATCH_ESVO;
@@ -1647,9 +1657,11 @@ __device__ __noinline__ uint32_t render_job_pixel(const BatchJob& J, uint32_t ix
         const float ec = __fdiv_rn(voxel_emission_coeff(f, rd), side);
         V3 total;
         if (J.layout == 1) {
-            total = J.tex_normalized
-                        ? trace_dda_tex<false, true>(J.tex, J.dim[0], J.dim[1], J.dim[2], ro, rd, loads, err)
-                        : trace_dda_tex<false, false>(J.tex, J.dim[0], J.dim[1], J.dim[2], ro, rd, loads, err);
+            total = J.tex_normalized == TEX_NORM
+                        ? trace_dda_tex<false, TEX_NORM>(J.tex, J.dim[0], J.dim[1], J.dim[2], ro, rd, loads, err)
+                    : J.tex_normalized == TEX_PACKED
+                        ? trace_dda_tex<false, TEX_PACKED>(J.tex, J.dim[0], J.dim[1], J.dim[2], ro, rd, loads, err)
+                        : trace_dda_tex<false, TEX_RAW>(J.tex, J.dim[0], J.dim[1], J.dim[2], ro, rd, loads, err);
         } else if (J.layout == 2) {
             const BrickGrid g{static_cast<const uint4*>(J.grid), J.dim[0], J.dim[1], J.dim[2], bricks_along(J.dim[0]),
                               bricks_along(J.dim[1])};
@@ -1732,8 +1744,12 @@ __device__ __forceinline__ uint32_t render_job_pixel_spec(const BatchJob& J, uin
             const float side = (float)m;
             const V3 ro = f.translation * side;
             const float ec = __fdiv_rn(voxel_emission_coeff(f, rd), side);
-            color = trace_dda_tex<false, SPEC == XN_BATCH_DDA_TEX_NORM>(J.tex, J.dim[0], J.dim[1], J.dim[2], ro, rd,
-                                                                        loads, err) * ec;
+            if (SPEC == XN_BATCH_DDA_TEX_NORM)
+                color = trace_dda_tex<false, TEX_NORM>(J.tex, J.dim[0], J.dim[1], J.dim[2], ro, rd, loads, err) * ec;
+            else if (J.tex_normalized == TEX_PACKED)
+                color = trace_dda_tex<false, TEX_PACKED>(J.tex, J.dim[0], J.dim[1], J.dim[2], ro, rd, loads, err) * ec;
+            else
+                color = trace_dda_tex<false, TEX_RAW>(J.tex, J.dim[0], J.dim[1], J.dim[2], ro, rd, loads, err) * ec;
         } else if constexpr (SPEC == XN_BATCH_ROPE) {
             color = trace_svo_job<XN_TRAV_SVO_ROPE>(RopeNodes{J.rinner, J.inner_depth, J.leaves}, f, rd, loads, err,
                                                     stk) *
@@ -1890,11 +1906,18 @@ cudaError_t launch_batch(const void* table, unsigned long long* q, uint32_t* err
 // renders it with the batch kernel's per-pixel code, and counts it done; the
 // warp that completes a job raises the job's flag in mapped host memory.
 // Every wait is bounded: a warp that finds nothing to claim sleeps (1 us,
-// doubling to 32 us while nothing comes) and looks again, and once the ring
-// has been idle for idle_ns the whole kernel exits (status bit 0), as it does
-// when the host closes the ring and every published tile is taken.  Jobs
-// published after that are found not done by the host and published again to
-// the next launch; re-rendering a tile writes the same pixels.
+// doubling to 32 us while nothing comes) and looks again.  A warp that has
+// found nothing for idle_ns raises the exit flag (status bit 0); from then on
+// no warp claims a tile, so the kernel leaves as soon as the tiles in hand are
+// done (were claims still taken, the warps that momentarily found nothing
+// would leave one by one while the rest kept taking newly published jobs, and
+// a kernel down to a few warps would hold the ring).  The decision is also
+// written to the flag after the ring's done flags in mapped host memory, so
+// the host publishes new jobs to the other ring at once.  A closed ring is
+// drained: every published tile is taken before the warps leave.  Jobs left
+// unfinished are found so by the host when the kernel has ended and are
+// published again to the next launch; re-rendering a tile writes the same
+// pixels.
 //
 // The polls are relaxed loads and the ring slots are read around L1 (.cg):
 // an acquire load would invalidate the SM's L1 on every poll, which the
@@ -1932,14 +1955,15 @@ __device__ __forceinline__ void load_job_cg(const BatchJob* src, BatchJob* dst, 
     __syncwarp();
 }
 
-constexpr uint32_t FOLD_THREADS = 128;
-
-template <int TW>
-__global__ void __launch_bounds__(FOLD_THREADS, 4) fold_kernel(FoldCtl* ctl, const BatchJob* ring, uint32_t cap,
+// Blocks of THREADS (32 or 128) threads: a one-warp block needs a quarter of
+// the registers and shared memory of a four-warp one, so it also fits where
+// a large frame's retiring block freed little.
+template <int TW, uint32_t THREADS>
+__global__ void __launch_bounds__(THREADS, 512 / THREADS) fold_kernel(FoldCtl* ctl, const BatchJob* ring, uint32_t cap,
                                                             uint32_t* done_tiles, volatile uint32_t* done_flags,
                                                             uint32_t* err_word, unsigned long long idle_ns) {
     fill_unorm_lut();
-    __shared__ BatchJob s_job[FOLD_THREADS / 32];
+    __shared__ BatchJob s_job[THREADS / 32];
     constexpr int TH = 32 / TW;
     extern __shared__ uint32_t batch_stacks[];
     SharedStacks stk{batch_stacks + threadIdx.x, batch_stacks + STACK_DEPTH * blockDim.x + threadIdx.x, blockDim.x};
@@ -1953,23 +1977,28 @@ __global__ void __launch_bounds__(FOLD_THREADS, 4) fold_kernel(FoldCtl* ctl, con
         unsigned long long t = ~0ull;
         int quit = 0;
         if (lane == 0) {
-            const unsigned long long pub = ld_relaxed_u64(&ctl->published);
-            unsigned long long cur = ld_relaxed_u64(&ctl->taken);
-            while (cur < pub) {
-                const unsigned long long prev = atomicCAS(&ctl->taken, cur, cur + 1);
-                if (prev == cur) {
-                    t = cur;
-                    break;
+            if (ld_relaxed_u32(&ctl->exit_flag)) {
+                quit = 1;  // the kernel is leaving: no new claims
+            } else {
+                const unsigned long long pub = ld_relaxed_u64(&ctl->published);
+                unsigned long long cur = ld_relaxed_u64(&ctl->taken);
+                while (cur < pub) {
+                    const unsigned long long prev = atomicCAS(&ctl->taken, cur, cur + 1);
+                    if (prev == cur) {
+                        t = cur;
+                        break;
+                    }
+                    cur = prev;
                 }
-                cur = prev;
-            }
-            if (t == ~0ull) {
-                if (ld_relaxed_u32(&ctl->closed) || ld_relaxed_u32(&ctl->exit_flag)) {
-                    quit = 1;
-                } else if (global_ns() - idle_since > idle_ns) {
-                    atomicExch(&ctl->exit_flag, 1u);
-                    atomicOr(&ctl->status, 1u);
-                    quit = 1;
+                if (t == ~0ull) {
+                    if (ld_relaxed_u32(&ctl->closed)) {
+                        quit = 1;
+                    } else if (global_ns() - idle_since > idle_ns) {
+                        atomicExch(&ctl->exit_flag, 1u);
+                        atomicOr(&ctl->status, 1u);
+                        done_flags[cap] = 1u;  // the host stops publishing to this ring
+                        quit = 1;
+                    }
                 }
             }
         }
@@ -2021,13 +2050,18 @@ __global__ void __launch_bounds__(FOLD_THREADS, 4) fold_kernel(FoldCtl* ctl, con
 }
 
 cudaError_t launch_fold(FoldCtl* ctl, const BatchJob* ring, uint32_t cap, uint32_t* done_tiles,
-                        uint32_t* done_flags_mapped, uint32_t* err, uint32_t tile_w, uint32_t blocks,
+                        uint32_t* done_flags_mapped, uint32_t* err, uint32_t tile_w, uint32_t threads, uint32_t blocks,
                         unsigned long long idle_ns, cudaStream_t s) {
-    const size_t smem = (size_t)2 * STACK_DEPTH * 4 * FOLD_THREADS;
-    if (tile_w == 4)
-        fold_kernel<4><<<blocks, FOLD_THREADS, smem, s>>>(ctl, ring, cap, done_tiles, done_flags_mapped, err, idle_ns);
+    if (threads != 32 && threads != 128) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)2 * STACK_DEPTH * 4 * threads;
+    if (tile_w == 4 && threads == 32)
+        fold_kernel<4, 32><<<blocks, 32, smem, s>>>(ctl, ring, cap, done_tiles, done_flags_mapped, err, idle_ns);
+    else if (tile_w == 4)
+        fold_kernel<4, 128><<<blocks, 128, smem, s>>>(ctl, ring, cap, done_tiles, done_flags_mapped, err, idle_ns);
+    else if (threads == 32)
+        fold_kernel<8, 32><<<blocks, 32, smem, s>>>(ctl, ring, cap, done_tiles, done_flags_mapped, err, idle_ns);
     else
-        fold_kernel<8><<<blocks, FOLD_THREADS, smem, s>>>(ctl, ring, cap, done_tiles, done_flags_mapped, err, idle_ns);
+        fold_kernel<8, 128><<<blocks, 128, smem, s>>>(ctl, ring, cap, done_tiles, done_flags_mapped, err, idle_ns);
     return cudaGetLastError();
 }
 

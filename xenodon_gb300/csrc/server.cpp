@@ -8,12 +8,14 @@
 //  - small frames (below fold_max_pixels) are folded into a persistent kernel
 //    while it runs: the worker appends each one to a job ring in device memory
 //    and raises the ring's published tile count (render.cu fold_kernel), on a
-//    high-priority stream.  The kernel claims tiles as they are published and
-//    flags each finished job in mapped host memory; the worker then copies
-//    that frame out at once, without waiting for the rest.  The kernel leaves
-//    after a short idle time (every device-side wait is bounded), and a ring
-//    whose slots are used up is closed while the other ring takes new jobs;
-//    jobs that reached a ring after its kernel left are published again;
+//    high-priority stream of that ring.  The kernel claims tiles as they are
+//    published and flags each finished job in mapped host memory; the worker
+//    then copies that frame out at once, without waiting for the rest.  The
+//    kernel leaves after a short idle time (every device-side wait is
+//    bounded) and says so in the same mapped memory; that ring, like one
+//    whose slots are used up, is closed and the other ring takes new jobs
+//    (on its own stream, so its kernel does not queue behind the leaving
+//    one); jobs a ring held when its kernel left are published again;
 //  - large frames (each fills the GPU alone) run through the single-frame
 //    kernels, each on one of `streams` low-priority streams (a few frames in
 //    flight, so one frame's last blocks overlap the next frame's first), and
@@ -136,12 +138,13 @@ struct FoldRing {
     xn::FoldCtl* d_ctl = nullptr;
     xn::BatchJob* d_ring = nullptr;
     uint32_t* d_done_tiles = nullptr;
-    uint32_t* h_done = nullptr;           // mapped pinned host memory, one flag per slot
+    uint32_t* h_done = nullptr;           // mapped pinned host memory: one flag per slot, then the leaving flag
     uint32_t* d_done_alias = nullptr;     // its device address
     xn::BatchJob* h_ring = nullptr;       // pinned
     unsigned long long* h_pub = nullptr;  // pinned: the published count after each slot
     uint32_t* h_one = nullptr;            // pinned constant 1 (the closed flag)
     cudaEvent_t ready = nullptr, ended = nullptr;
+    cudaStream_t stream = nullptr;        // high priority; one per ring, so a new kernel never queues behind a leaving one
     uint32_t n = 0;
     unsigned long long tiles = 0;
     bool launched = false, closed = false;
@@ -171,7 +174,7 @@ struct xn_server {
     std::vector<Request*> copying;    // D2H copies in flight (an event each)
     std::deque<Request*> copy_queue;  // copied to staging; the copy thread finishes them
     std::vector<Request*> large_inflight;
-    cudaStream_t fold_stream = nullptr, ctl_stream = nullptr, copy_stream = nullptr;
+    cudaStream_t ctl_stream = nullptr, copy_stream = nullptr;
     std::vector<cudaStream_t> large_streams;  // low priority, one per large frame in flight
     size_t next_large = 0;
     FoldRing rings[FOLD_RINGS];
@@ -190,6 +193,8 @@ struct xn_server {
     // from submit to launch, launch to done on the GPU, to copied, to done)
     std::string trace_path;
     std::vector<std::string> trace;
+    // XN_FOLD_THREADS=32|128: threads per block of the persistent kernel
+    uint32_t fold_threads = 128;
 
     void run();
     void copy_run();
@@ -325,7 +330,7 @@ int xn_server::reset_ring(FoldRing& r) {
     cudaError_t e = cudaMemsetAsync(r.d_ring, 0xFF, (size_t)cfg.max_batch_jobs * sizeof(xn::BatchJob), ctl_stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(r.d_ctl, 0, sizeof(xn::FoldCtl), ctl_stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(r.d_done_tiles, 0, (size_t)cfg.max_batch_jobs * 4, ctl_stream);
-    std::memset(r.h_done, 0, (size_t)cfg.max_batch_jobs * 4);
+    std::memset(r.h_done, 0, ((size_t)cfg.max_batch_jobs + 1) * 4);
     r.n = 0;
     r.tiles = 0;
     r.launched = r.closed = false;
@@ -427,6 +432,11 @@ bool xn_server::poll_copies() {
 void xn_server::publish_small() {
     while (!pending_small.empty()) {
         FoldRing& r = rings[cur_ring];
+        if (r.launched && !r.closed && reinterpret_cast<volatile uint32_t*>(r.h_done)[cfg.max_batch_jobs]) {
+            // its kernel has decided to leave and takes no new tiles: what it
+            // still holds is published again once it has ended
+            r.closed = true;
+        }
         if (r.closed) {
             // the other ring takes over once its kernel has left and it was reset
             const int other = (cur_ring + 1) % FOLD_RINGS;
@@ -469,13 +479,16 @@ void xn_server::publish_small() {
             e = cudaMemcpyAsync(&r.d_ctl->published, r.h_pub + k, 8, cudaMemcpyHostToDevice, ctl_stream);
         if (e == cudaSuccess && !r.launched) {
             e = cudaEventRecord(r.ready, ctl_stream);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(fold_stream, r.ready, 0);
-            const uint32_t blocks = 2u * (uint32_t)c->sm_count() * std::max(1u, cfg.fold_blocks_per_sm);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(r.stream, r.ready, 0);
+            // fold_blocks_per_sm x 8 warps per SM, in blocks of fold_threads
+            const uint32_t blocks =
+                2u * (uint32_t)c->sm_count() * std::max(1u, cfg.fold_blocks_per_sm) * (128u / fold_threads);
             if (e == cudaSuccess)
                 e = xn::launch_fold(r.d_ctl, r.d_ring, (uint32_t)cfg.max_batch_jobs, r.d_done_tiles, r.d_done_alias,
-                                    c->d_err, FOLD_TILE_W, blocks, (unsigned long long)cfg.fold_idle_us * 1000ull,
-                                    fold_stream);
-            if (e == cudaSuccess) e = cudaEventRecord(r.ended, fold_stream);
+                                    c->d_err, FOLD_TILE_W, fold_threads, blocks,
+                                    (unsigned long long)cfg.fold_idle_us * 1000ull,
+                                    r.stream);
+            if (e == cudaSuccess) e = cudaEventRecord(r.ended, r.stream);
             if (e == cudaSuccess) {
                 r.launched = true;
                 ++fold_launches;
@@ -484,7 +497,7 @@ void xn_server::publish_small() {
         }
         if (e != cudaSuccess) {  // the ring is unusable: fail what it holds
             cudaStreamSynchronize(ctl_stream);
-            cudaStreamSynchronize(fold_stream);
+            cudaStreamSynchronize(r.stream);
             for (uint32_t i = 0; i <= k; ++i)
                 if (r.req[i] && !r.collected[i]) {
                     unadmit(r.req[i]);
@@ -643,6 +656,7 @@ XN_API int xn_server_create(xn_ctx* ctx, const xn_server_config* cfg, xn_server*
     if (s->cfg.fold_blocks_per_sm > 2) s->cfg.fold_blocks_per_sm = 2;
     s->host_pool.device = false;
     if (const char* tp = std::getenv("XN_SERVER_TRACE")) s->trace_path = tp;
+    if (const char* ft = std::getenv("XN_FOLD_THREADS")) s->fold_threads = std::atoi(ft) == 32 ? 32u : 128u;
     uint64_t used = 0, budget = 0;
     xn_ctx_memory(ctx, &used, &budget);
     s->budget = s->cfg.hbm_budget ? s->cfg.hbm_budget : budget;
@@ -652,8 +666,7 @@ XN_API int xn_server_create(xn_ctx* ctx, const xn_server_config* cfg, xn_server*
     }
     int lo = 0, hi = 0;  // numerically lower is more urgent
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
-    bool ok = cudaStreamCreateWithPriority(&s->fold_stream, cudaStreamNonBlocking, hi) == cudaSuccess &&
-              cudaStreamCreateWithFlags(&s->ctl_stream, cudaStreamNonBlocking) == cudaSuccess &&
+    bool ok = cudaStreamCreateWithFlags(&s->ctl_stream, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithPriority(&s->copy_stream, cudaStreamNonBlocking, hi) == cudaSuccess;
     for (int i = 0; ok && i < s->cfg.streams; ++i) {
         cudaStream_t st = nullptr;
@@ -666,7 +679,8 @@ XN_API int xn_server_create(xn_ctx* ctx, const xn_server_config* cfg, xn_server*
         ok = cudaMalloc(reinterpret_cast<void**>(&r.d_ctl), sizeof(xn::FoldCtl)) == cudaSuccess &&
              cudaMalloc(reinterpret_cast<void**>(&r.d_ring), cap * sizeof(xn::BatchJob)) == cudaSuccess &&
              cudaMalloc(reinterpret_cast<void**>(&r.d_done_tiles), cap * 4) == cudaSuccess &&
-             cudaHostAlloc(reinterpret_cast<void**>(&r.h_done), cap * 4, cudaHostAllocMapped) == cudaSuccess &&
+             cudaStreamCreateWithPriority(&r.stream, cudaStreamNonBlocking, hi) == cudaSuccess &&
+             cudaHostAlloc(reinterpret_cast<void**>(&r.h_done), (cap + 1) * 4, cudaHostAllocMapped) == cudaSuccess &&
              cudaHostGetDevicePointer(reinterpret_cast<void**>(&r.d_done_alias), r.h_done, 0) == cudaSuccess &&
              cudaHostAlloc(reinterpret_cast<void**>(&r.h_ring), cap * sizeof(xn::BatchJob), cudaHostAllocDefault) ==
                  cudaSuccess &&
@@ -714,8 +728,10 @@ XN_API int xn_server_destroy(xn_server* s) {
     if (s->copier.joinable()) s->copier.join();
     s->cv_done.notify_all();
     cudaSetDevice(s->c->device);
-    for (cudaStream_t st : {s->fold_stream, s->ctl_stream, s->copy_stream})
+    for (cudaStream_t st : {s->ctl_stream, s->copy_stream})
         if (st) cudaStreamSynchronize(st);
+    for (auto& r : s->rings)
+        if (r.stream) cudaStreamSynchronize(r.stream);
     for (cudaStream_t st : s->large_streams) cudaStreamSynchronize(st);
     for (auto& kv : s->volumes)
         if (kv.second.dev && !kv.second.external) xn_volume_release(kv.second.dev);
@@ -729,11 +745,12 @@ XN_API int xn_server_destroy(xn_server* s) {
         if (r.h_one) cudaFreeHost(r.h_one);
         if (r.ready) cudaEventDestroy(r.ready);
         if (r.ended) cudaEventDestroy(r.ended);
+        if (r.stream) cudaStreamDestroy(r.stream);
     }
     s->dev_pool.release();
     s->host_pool.release();
     for (cudaEvent_t e : s->event_pool) cudaEventDestroy(e);
-    for (cudaStream_t st : {s->fold_stream, s->ctl_stream, s->copy_stream})
+    for (cudaStream_t st : {s->ctl_stream, s->copy_stream})
         if (st) cudaStreamDestroy(st);
     for (cudaStream_t st : s->large_streams) cudaStreamDestroy(st);
     for (auto& kv : s->requests) delete kv.second;

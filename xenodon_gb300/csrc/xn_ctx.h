@@ -57,7 +57,7 @@ struct Volume {
     // grid texture form (xn_volume_upload_grid)
     cudaArray_t array = nullptr;
     cudaTextureObject_t tex = 0;
-    int tex_normalized = 0;
+    int tex_normalized = 0;  // texel form: 0 bytes (converted in the kernel), 1 byte/255 from the texture unit, 2 one packed word
     int bricked = 0;  // grid kept in the bricked form (XN_GRID_LAYOUT=bricked)
     int hybrid = 0;   // texture plus an x-fastest copy (XN_GRID_LAYOUT=hybrid)
     uint64_t array_bytes = 0;

@@ -76,6 +76,19 @@ __device__ __forceinline__ float unorm8(uint32_t c) {
 __device__ __forceinline__ V3 unpack_rgb(uint32_t col) {
     return V3{unorm8(col & 0xFFu), unorm8((col >> 8) & 0xFFu), unorm8((col >> 16) & 0xFFu)};
 }
+// The same values with the byte's float made without a conversion
+// instruction: 2^23 + c has c in its low mantissa bits, and subtracting 2^23
+// is exact, so cf equals the converted byte.
+__device__ __forceinline__ float unorm8_bits(uint32_t c) {
+    const float r = 1.0f / 255.0f;
+    const float cf = __uint_as_float(0x4B000000u | c) - 8388608.0f;
+    const float q0 = cf * r;
+    const float rem = fmaf(-q0, 255.0f, cf);
+    return fmaf(rem, r, q0);
+}
+__device__ __forceinline__ V3 unpack_rgb_bits(uint32_t col) {
+    return V3{unorm8_bits(col & 0xFFu), unorm8_bits((col >> 8) & 0xFFu), unorm8_bits((col >> 16) & 0xFFu)};
+}
 
 // resources/common.glsl:40-43
 __device__ __forceinline__ V3 adjust_ray(V3 rd) {

@@ -37,7 +37,7 @@ struct RenderLaunch {
     // volume
     const void* grid;   // uchar4 texels, x fastest (DDA, linear form)
     unsigned long long tex;  // cudaTextureObject_t of the texture form, or 0
-    int tex_normalized;      // the texture returns byte/255 itself
+    int tex_normalized;      // 1: the texture returns byte/255 itself; 0: four bytes; 2: one packed word
     int grid_bricked;        // `grid` is the bricked form (render.cu BrickGrid), not x-fastest
     int grid_hybrid;         // both `tex` and an x-fastest `grid`: some warps read each (render.cu)
     uint32_t dim[3];
@@ -123,15 +123,16 @@ struct alignas(16) FoldCtl {
     unsigned long long published;  // tiles published (host writes, by copy)
     unsigned long long taken;      // tiles claimed (device)
     uint32_t closed;               // host: no more jobs; exit once every published tile is taken
-    uint32_t exit_flag;            // device: the ring went idle; every warp leaves
+    uint32_t exit_flag;            // device: the ring went idle; no warp claims a tile after it
     uint32_t status;               // device: bit 0, left because idle
     uint32_t pad;
 };
-// Launches the persistent folding kernel (128 threads a block, the generic
-// per-pixel form, warp tiles of tile_w x 32/tile_w) over a ring of `cap`
-// job slots; done_flags is mapped host memory (one word per slot).
+// Launches the persistent folding kernel (blocks of `threads`, 32 or 128;
+// the generic per-pixel form, warp tiles of tile_w x 32/tile_w) over a ring
+// of `cap` job slots; done_flags is mapped host memory: one word per slot,
+// then one word the kernel sets when it decides to leave.
 cudaError_t launch_fold(FoldCtl* ctl, const BatchJob* ring, uint32_t cap, uint32_t* done_tiles,
-                        uint32_t* done_flags_mapped, uint32_t* err, uint32_t tile_w, uint32_t blocks,
+                        uint32_t* done_flags_mapped, uint32_t* err, uint32_t tile_w, uint32_t threads, uint32_t blocks,
                         unsigned long long idle_ns, cudaStream_t s);
 
 }  // namespace xn
