@@ -276,7 +276,7 @@ typedef struct {
     int streams;           /* large frames in flight at once, one stream each (default 2, at most 16) */
     uint64_t fold_max_pixels;    /* frames below this many pixels are folded (0: 2^19) */
     uint32_t fold_idle_us;       /* the persistent kernel leaves after this long without work (0: 300) */
-    uint32_t fold_blocks_per_sm; /* its warps per SM in units of 8 (blocks of 128 threads), 1 or 2 (0: 1) */
+    uint32_t fold_blocks_per_sm; /* its blocks of 4 warps per SM, 1 to 4 (0: 2) */
     uint64_t band_pixels;  /* large frames are launched in bands of rows of about this many pixels (0: whole) */
 } xn_server_config;
 typedef struct {

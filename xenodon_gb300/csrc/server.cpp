@@ -480,9 +480,9 @@ void xn_server::publish_small() {
         if (e == cudaSuccess && !r.launched) {
             e = cudaEventRecord(r.ready, ctl_stream);
             if (e == cudaSuccess) e = cudaStreamWaitEvent(r.stream, r.ready, 0);
-            // fold_blocks_per_sm x 8 warps per SM, in blocks of fold_threads
+            // fold_blocks_per_sm x 4 warps per SM, in blocks of fold_threads
             const uint32_t blocks =
-                2u * (uint32_t)c->sm_count() * std::max(1u, cfg.fold_blocks_per_sm) * (128u / fold_threads);
+                (uint32_t)c->sm_count() * std::max(1u, cfg.fold_blocks_per_sm) * (128u / fold_threads);
             if (e == cudaSuccess)
                 e = xn::launch_fold(r.d_ctl, r.d_ring, (uint32_t)cfg.max_batch_jobs, r.d_done_tiles, r.d_done_alias,
                                     c->d_err, FOLD_TILE_W, fold_threads, blocks,
@@ -652,8 +652,8 @@ XN_API int xn_server_create(xn_ctx* ctx, const xn_server_config* cfg, xn_server*
     if (s->cfg.streams > 16) s->cfg.streams = 16;
     if (s->cfg.fold_max_pixels == 0) s->cfg.fold_max_pixels = 1ull << 19;
     if (s->cfg.fold_idle_us == 0) s->cfg.fold_idle_us = 300;
-    if (s->cfg.fold_blocks_per_sm == 0) s->cfg.fold_blocks_per_sm = 1;
-    if (s->cfg.fold_blocks_per_sm > 2) s->cfg.fold_blocks_per_sm = 2;
+    if (s->cfg.fold_blocks_per_sm == 0) s->cfg.fold_blocks_per_sm = 2;
+    if (s->cfg.fold_blocks_per_sm > 4) s->cfg.fold_blocks_per_sm = 4;
     s->host_pool.device = false;
     if (const char* tp = std::getenv("XN_SERVER_TRACE")) s->trace_path = tp;
     if (const char* ft = std::getenv("XN_FOLD_THREADS")) s->fold_threads = std::atoi(ft) == 32 ? 32u : 128u;
