@@ -184,13 +184,15 @@ XN_API int xn_render_device(xn_ctx* ctx, const xn_volume* vol, int traversal, co
  * caller renders the next frame into a second output while it encodes this
  * one.
  *   xn_output_create   an output of up to max_pixels pixels (device image,
- *                      pinned host image, events, error word)
+ *                      pinned host image, events, error word, copy stream)
  *   xn_output_render   queues the render of params->output_region (at most
  *                      max_pixels pixels) on the context's stream, timed by
- *                      events, then the copy into the pinned image (skipped
- *                      with XN_OUTPUT_DISCARD, the reference's
- *                      --discard-output); returns at once.  The previous
- *                      render into this output must have been waited for.
+ *                      events, then the copy into the pinned image on the
+ *                      output's own stream, so the next render's kernel does
+ *                      not wait for it (the copy is skipped with
+ *                      XN_OUTPUT_DISCARD, the reference's --discard-output);
+ *                      returns at once.  The previous render into this output
+ *                      must have been waited for.
  *   xn_output_wait     the fence: blocks until the queued render and copy are
  *                      done; *rgba (width*height*4 bytes, row pitch width*4)
  *                      stays valid until the next xn_output_render on this

@@ -78,3 +78,32 @@ def test_output_misuse_is_refused(ctx):
     finally:
         lib.xn_output_destroy(o)
         vg.release()
+
+
+def test_output_wrapper_pipeline_into_caller_buffers(ctx):
+    """Output (the Python face of xn_output): each frame is copied on the
+    output's own stream while the next frame renders; frames taken into the
+    caller's buffers equal xn_render's, for every traversal."""
+    import xenodon_gb300 as xg
+    from xenodon_gb300 import cameras, volumes
+    g = volumes.blobs(64, seed=5)
+    nodes, st = ctx.build_svo(g, "rope")
+    vg, vs = ctx.upload_grid(g), ctx.upload_svo(nodes, st["side"])
+    w, h = 640, 360
+    params = xg.make_params(w, h, emission_coeff=10.0)
+    path = cameras.orbit(np.array([0.5, 0.5, 0.5]), 1.6, 4)
+    jobs = [(t, c) for c in path for t in xg.TRAVERSALS]
+    got = [np.empty((h, w, 4), np.uint8) for _ in jobs]
+    with xg.Output(ctx, w * h) as a, xg.Output(ctx, w * h) as b:
+        outs, pending = (a, b), None
+        for i, (t, c) in enumerate(jobs):
+            outs[i % 2].render(vg if t == "dda" else vs, t, xg.make_camera(*c), params)
+            if pending is not None:
+                pending[0].wait(out=got[pending[1]])
+            pending = (outs[i % 2], i)
+        pending[0].wait(out=got[pending[1]])
+    for (t, c), img in zip(jobs, got):
+        want, _, _ = ctx.render(vg if t == "dda" else vs, t, xg.make_camera(*c), params)
+        assert np.array_equal(img, want), t
+    vg.release()
+    vs.release()

@@ -22,6 +22,7 @@ TRAVERSALS = {"dda": 0, "svo-naive": 1, "esvo": 2, "svo-df": 3, "svo-rope": 4}
 SVO_TRAVERSALS = ("svo-naive", "esvo", "svo-df", "svo-rope")
 SVO_TYPES = {"sparse": 0, "dag": 1, "rope": 2}
 XN_BUILD_LEAN = 0x100  # xn_build_svo_volume: write the device layout directly (sparse trees)
+XN_OUTPUT_DISCARD = 1  # xn_output_render: no read-back
 HEURISTICS = {"chan-diff": 0, "std-dev": 1}
 
 XN_OK = 0
@@ -447,6 +448,52 @@ class BatchGraph:
             self.close()
         except Exception:
             pass
+
+
+class Output:
+    """xn_output: renders queued on the context's stream, each frame copied
+    into pinned host memory on the output's own stream; wait() is the fence.
+    Two outputs used in turn keep the GPU busy while the host takes the
+    previous frame."""
+
+    def __init__(self, ctx: "Context", max_pixels: int):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = ctypes.c_void_p()
+        _check(self.lib.xn_output_create(ctx.handle, int(max_pixels), ctypes.byref(h)))
+        self.handle = h
+        self._shape = None
+
+    def render(self, vol: "Volume", traversal: str, camera: Camera, params: Params, discard: bool = False) -> None:
+        _check(self.lib.xn_output_render(self.handle, vol.handle, _traversal(traversal), ctypes.byref(camera),
+                                         ctypes.byref(params), XN_OUTPUT_DISCARD if discard else 0))
+        self._shape = (params.output_region.height, params.output_region.width, 4)
+
+    def wait(self, out: np.ndarray | None = None):
+        """Blocks until the queued render and copy are done; copies the frame
+        into `out` (uint8, height x width x 4) when given and returns
+        (image, kernel ms).  Without `out` the image is a view of the pinned
+        buffer, valid until the next render into this output."""
+        px = ctypes.POINTER(ctypes.c_uint8)()
+        ms = ctypes.c_float()
+        _check(self.lib.xn_output_wait(self.handle, ctypes.byref(px), ctypes.byref(ms)))
+        h, w, c = self._shape
+        view = np.ctypeslib.as_array(px, shape=(h * w * c,)).reshape(h, w, c)
+        if out is not None:
+            np.copyto(out, view)
+            return out, ms.value
+        return view, ms.value
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.xn_output_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 class Server:

@@ -3,10 +3,12 @@
 // (src/backend/headless/HeadlessOutput.cpp:38-136).  The reference waits on
 // the fence and then copies the image through a mapped staging buffer, one
 // row at a time, before the next frame is recorded (HeadlessOutput.cpp:90-136,
-// HeadlessDisplay.cpp:39-54).  Here a render queues the kernel and an
-// asynchronous copy into pinned host memory and returns; the wait is an event
-// synchronisation, so a caller with two outputs per region encodes frame n
-// while frame n+1 renders.
+// HeadlessDisplay.cpp:39-54).  Here a render queues the kernel on the
+// context's stream and the copy into pinned host memory on the output's own
+// copy stream (after an event), and returns; the wait is an event
+// synchronisation.  So the next render's kernel runs while this frame is
+// copied, and a caller with two outputs per region encodes frame n while
+// frame n+1 renders.
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -30,6 +32,7 @@ struct Output {
     uint32_t* d_err = nullptr;      // this output's ray error bits
     uint32_t* h_err = nullptr;      // pinned copy
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, done = nullptr;
+    cudaStream_t copy = nullptr;    // this output's device-to-host copies
     bool pending = false;           // a render was queued and not yet waited for
 };
 
@@ -57,6 +60,7 @@ XN_API int xn_output_create(xn_ctx* h, uint64_t max_pixels, xn_output** out) {
         if (o->ev0) cudaEventDestroy(o->ev0);
         if (o->ev1) cudaEventDestroy(o->ev1);
         if (o->done) cudaEventDestroy(o->done);
+        if (o->copy) cudaStreamDestroy(o->copy);
         delete o;
         return code;
     };
@@ -67,6 +71,7 @@ XN_API int xn_output_create(xn_ctx* h, uint64_t max_pixels, xn_output** out) {
     if (e == cudaSuccess) e = cudaEventCreate(&o->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&o->ev1);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&o->done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&o->copy, cudaStreamNonBlocking);
     if (e != cudaSuccess) return undo(cuda_fail(e, "xn_output_create"));
     *o->h_err = 0;
     *out = reinterpret_cast<xn_output*>(o);
@@ -99,10 +104,13 @@ XN_API int xn_output_render(xn_output* oh, const xn_volume* vh, int traversal, c
     if (e == cudaSuccess) e = cudaEventRecord(o->ev0, c->stream);
     if (e == cudaSuccess) e = launch_render(L, c->stream);
     if (e == cudaSuccess) e = cudaEventRecord(o->ev1, c->stream);
+    // the copies wait for the kernel on the output's stream, so the context's
+    // stream is free for the next render meanwhile
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(o->copy, o->ev1, 0);
     if (e == cudaSuccess && !(flags & XN_OUTPUT_DISCARD))
-        e = cudaMemcpyAsync(o->h_rgba, o->d_rgba, npix * 4, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(o->h_err, o->d_err, 4, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaEventRecord(o->done, c->stream);
+        e = cudaMemcpyAsync(o->h_rgba, o->d_rgba, npix * 4, cudaMemcpyDeviceToHost, o->copy);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(o->h_err, o->d_err, 4, cudaMemcpyDeviceToHost, o->copy);
+    if (e == cudaSuccess) e = cudaEventRecord(o->done, o->copy);
     if (e != cudaSuccess) return cuda_fail(e, "xn_output_render");
     o->pending = true;
     return XN_OK;
@@ -138,6 +146,7 @@ XN_API int xn_output_destroy(xn_output* oh) {
     cudaEventDestroy(o->ev0);
     cudaEventDestroy(o->ev1);
     cudaEventDestroy(o->done);
+    cudaStreamDestroy(o->copy);
     delete o;
     return XN_OK;
 }
