@@ -27,3 +27,26 @@ def test_reference_arm_prints_one_contract_line():
     e = d["e2e"]
     assert e["value"] == d["value"] and e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
     assert d["config"]["volume"] == [512, 361, 512] and d["config"]["resolution"] == [1920, 1080]
+
+
+def test_committed_profile_figures_cover_every_traversal():
+    """The DRAM traffic and the issue/ALU figures the bench line carries come
+    from the committed ncu summaries; every traversal has both, and the
+    values are plausible (bytes per launch, fractions of peak)."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    traffic, issue = bench.load_traffic(), bench.load_issue()
+    trav = {"dda", "svo-naive", "esvo", "svo-df", "svo-rope"}
+    assert set(traffic) == trav and set(issue) == trav
+    assert all(1e6 < v < 1e10 for v in traffic.values())
+    for v in issue.values():
+        assert 0.0 < v["issue_active_frac"] <= 1.0 and 0.0 < v["alu_pipe_frac"] <= 1.0
+
+
+def test_cpu_sample_bands_stay_inside_the_frame():
+    sys.path.insert(0, str(ROOT))
+    import bench
+    for bands, rows in ((16, 64), (4, 64), (1, 8), (40, 64)):
+        offs = bench.band_offsets(bands, rows)
+        assert offs == sorted(offs) and offs[0] >= 0 and offs[-1] + rows <= bench.HEIGHT
+        assert all(b - a >= rows for a, b in zip(offs, offs[1:]))
