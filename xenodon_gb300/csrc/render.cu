@@ -163,7 +163,7 @@ __device__ V3 trace_dda_tex(cudaTextureObject_t tex, uint32_t dx, uint32_t dy, u
         if (COUNT) ++loads;
         // lessThanEqual(side, min(side.yzx, side.zxy)) is side.k == min of
         // all three (the sides are finite and positive)
-        const float t0 = fminf(side.x, fminf(side.y, side.z));
+        const float t0 = min3f(side.x, side.y, side.z);
         if (side.x == t0) { side.x = side.x + t_delta.x; px += sgn.x; }
         if (side.y == t0) { side.y = side.y + t_delta.y; py += sgn.y; }
         if (side.z == t0) { side.z = side.z + t_delta.z; pz += sgn.z; }
@@ -272,7 +272,7 @@ __device__ V3 trace_dda_brick(const BrickGrid& g, V3 ro, V3 rd, uint32_t& loads,
     while (t < lim) {
         if (++iter > cap) { err |= 1u; break; }
         if (COUNT) ++loads;
-        const float t0 = fminf(side.x, fminf(side.y, side.z));
+        const float t0 = min3f(side.x, side.y, side.z);
         if (side.x == t0) { side.x = side.x + t_delta.x; px += sx; }
         if (side.y == t0) { side.y = side.y + t_delta.y; py += sy; }
         if (side.z == t0) { side.z = side.z + t_delta.z; pz += sz; }
@@ -623,27 +623,21 @@ __device__ __forceinline__ ChildSlabs child_slabs(V3 origin, float s, V3 rrd, V3
 // max(t_min, 0) / t_max of child k, as the reference computes them for that box
 __device__ __forceinline__ void child_span(const ChildSlabs& c, uint32_t k, float& t0, float& t1) {
     const bool bx = k & 4u, by = k & 2u, bz = k & 1u;
-    t0 = fmaxf(bx ? c.xl1 : c.xl0, fmaxf(by ? c.yl1 : c.yl0, bz ? c.zl1 : c.zl0));
-    t1 = fminf(bx ? c.xh1 : c.xh0, fminf(by ? c.yh1 : c.yh0, bz ? c.zh1 : c.zh0));
+    t0 = max3f(bx ? c.xl1 : c.xl0, by ? c.yl1 : c.yl0, bz ? c.zl1 : c.zl0);
+    t1 = min3f(bx ? c.xh1 : c.xh0, by ? c.yh1 : c.yh0, bz ? c.zh1 : c.zh0);
 }
 
 // fmaxf/fminf are exact and the slab values are finite (every ray direction
-// component is at least 2^-23 in magnitude), so the per-child max/min may be
-// grouped as max(max(x, y), z): the x-y part is shared by the two children
-// that differ only in z.
+// component is at least 2^-23 in magnitude), so each child's max/min of
+// three is one three-input operation.
 __device__ __forceinline__ uint32_t hit_mask(const ChildSlabs& c) {
     uint32_t m = 0;
 #pragma unroll
-    for (uint32_t xy = 0; xy < 4; ++xy) {
-        const bool bx = xy & 2u, by = xy & 1u;
-        const float lo = fmaxf(bx ? c.xl1 : c.xl0, by ? c.yl1 : c.yl0);
-        const float hi = fminf(bx ? c.xh1 : c.xh0, by ? c.yh1 : c.yh0);
-#pragma unroll
-        for (uint32_t bz = 0; bz < 2; ++bz) {
-            const float t0 = fmaxf(lo, bz ? c.zl1 : c.zl0);
-            const float t1 = fminf(hi, bz ? c.zh1 : c.zh0);
-            if (t0 < t1) m |= 1u << (xy * 2u + bz);  // t0 >= 0: t_max > 0 follows
-        }
+    for (uint32_t k = 0; k < 8; ++k) {
+        const bool bx = k & 4u, by = k & 2u, bz = k & 1u;
+        const float t0 = max3f(bx ? c.xl1 : c.xl0, by ? c.yl1 : c.yl0, bz ? c.zl1 : c.zl0);
+        const float t1 = min3f(bx ? c.xh1 : c.xh0, by ? c.yh1 : c.yh0, bz ? c.zh1 : c.zh0);
+        if (t0 < t1) m |= 1u << k;  // t0 >= 0: t_max > 0 follows
     }
     return m;
 }
@@ -962,7 +956,7 @@ __device__ __forceinline__ float aabb_entry(V3 bmin, V3 bmax, V3 ro, V3 rd) {
     V3 tbot = (bmin - ro) * rrd;
     V3 ttop = (bmax - ro) * rrd;
     V3 tmin = vmin(ttop, tbot);
-    return fmaxf(fmaxf(tmin.x, tmin.y), fmaxf(tmin.x, tmin.z));
+    return max3f(tmin.x, tmin.y, tmin.z);  // the same value as the reference's max(max(x, y), max(x, z))
 }
 
 // ---------------------------------------------------------------- kernels ---

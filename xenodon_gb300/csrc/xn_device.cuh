@@ -27,8 +27,21 @@ __device__ __forceinline__ V3 operator-(V3 a) { return V3{-a.x, -a.y, -a.z}; }
 __device__ __forceinline__ V3 vmin(V3 a, V3 b) { return V3{fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)}; }
 __device__ __forceinline__ V3 vmax(V3 a, V3 b) { return V3{fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z)}; }
 // resources/common.glsl:58-64
-__device__ __forceinline__ float min_elem(V3 v) { return fminf(v.x, fminf(v.y, v.z)); }
-__device__ __forceinline__ float max_elem(V3 v) { return fmaxf(v.x, fmaxf(v.y, v.z)); }
+// Three-input minimum and maximum (PTX min.f32 / max.f32 with three
+// sources): the value of fminf(a, fminf(b, c)), resp. fmaxf, for the finite,
+// non-NaN operands every caller passes, in one operation instead of two.
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float min_elem(V3 v) { return min3f(v.x, v.y, v.z); }
+__device__ __forceinline__ float max_elem(V3 v) { return max3f(v.x, v.y, v.z); }
 __device__ __forceinline__ float dot3(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
 __device__ __forceinline__ V3 cross3(V3 a, V3 b) {
     return V3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
