@@ -696,8 +696,8 @@ __device__ V3 trace_df_masked(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint3
                 inv = __frcp_rn(s2);
                 ex = pow2_with_normal_reciprocal(s2);
             }
-            origin = origin - v3(gl_mod_pow2(origin.x, s2, inv, ex), gl_mod_pow2(origin.y, s2, inv, ex),
-                                 gl_mod_pow2(origin.z, s2, inv, ex));
+            origin = v3(snap_down_pow2(origin.x, s2, inv, ex), snap_down_pow2(origin.y, s2, inv, ex),
+                        snap_down_pow2(origin.z, s2, inv, ex));
             slabs = child_slabs(origin, side, rrd, bias);
             continue;
         }
@@ -803,7 +803,11 @@ __device__ V3 trace_esvo(const Acc& a, V3 ro, V3 rd, uint32_t& loads, uint32_t& 
                 parent = child;
                 --scale;
                 scale_exp2 *= 0.5f;
-                V3 t_center = t_coeff * scale_exp2 + t_corner;
+                // t_coeff * scale_exp2 is exact (a power of two, 2^-23..2^-1,
+                // times |t_coeff| in [1, 2^23]), so the fused form rounds
+                // once, like the reference's product-then-sum
+                V3 t_center = v3(__fmaf_rn(t_coeff.x, scale_exp2, t_corner.x), __fmaf_rn(t_coeff.y, scale_exp2, t_corner.y),
+                                 __fmaf_rn(t_coeff.z, scale_exp2, t_corner.z));
                 bool ax = t_center.x > t_min, ay = t_center.y > t_min, az = t_center.z > t_min;
                 idx = cxor(0u, ax, ay, az);
                 if (ax) pos.x = pos.x + scale_exp2;
@@ -861,8 +865,8 @@ __device__ __forceinline__ uint32_t find_relative(const Acc& a, uint32_t parent,
     } else {
         extent = ldexpf(1.0f, -(int)(d > 1000u ? 1000u : d));
     }
-    offset = v3(offset.x - gl_mod_pow2(offset.x, extent, inv, ex), offset.y - gl_mod_pow2(offset.y, extent, inv, ex),
-                offset.z - gl_mod_pow2(offset.z, extent, inv, ex));
+    offset = v3(snap_down_pow2(offset.x, extent, inv, ex), snap_down_pow2(offset.y, extent, inv, ex),
+                snap_down_pow2(offset.z, extent, inv, ex));
     for (int level = 0;; ++level) {
         if (COUNT) ++loads;
         if (a.is_leaf(parent)) {

@@ -61,6 +61,14 @@ __device__ __forceinline__ float gl_mod(float x, float y) { return x - y * floor
 __device__ __forceinline__ float gl_mod_pow2(float x, float y, float inv, bool exact) {
     return x - y * floorf(exact ? x * inv : __fdiv_rn(x, y));
 }
+// x - mod(x, y), the reference's snap of x down to a multiple of y.  On the
+// exact path (y a power of two with a normal reciprocal) the remainder
+// r = x - y*floor(x/y) is exact -- a multiple of the smaller of y and x's ulp,
+// below y in magnitude -- so x - r is y*floor(x/y) exactly, with the same
+// sign of zero: three operations instead of five.
+__device__ __forceinline__ float snap_down_pow2(float x, float y, float inv, bool exact) {
+    return exact ? y * floorf(x * inv) : x - gl_mod_pow2(x, y, inv, false);
+}
 // Whether y is a power of two whose reciprocal is a normal float.
 __device__ __forceinline__ bool pow2_with_normal_reciprocal(float y) {
     const uint32_t b = __float_as_uint(y);
