@@ -1184,19 +1184,22 @@ struct PacketStacksColumns {
 // loops over the largest per-lane count instead of the union.
 
 // The hit leaves of node c (origin co, child size cs; all children leaves),
-// in index order.
+// in index order.  The eight children are tested in an unrolled loop, so
+// each child's span is formed from the slabs without a select on a run-time
+// index, and a hit leaf is accumulated where it is found: the same spans,
+// the same hit test and the same order as the hit mask and its walk.
 template <bool COUNT, class Acc>
 __device__ __forceinline__ void lane_leaves(const Acc& a, uint32_t c, V3 co, float cs, V3 rrd, V3 bias, V3& total,
                                             uint32_t& loads) {
     const ChildSlabs sl = child_slabs(co, cs, rrd, bias);
-    uint32_t m = hit_mask(sl);
-    while (m != 0) {
-        const uint32_t j = __ffs(m) - 1;
-        m &= m - 1;
+#pragma unroll
+    for (uint32_t j = 0; j < 8; ++j) {
         float t0, t1;
         child_span(sl, j, t0, t1);
-        if (COUNT) loads += 2;  // the leaf's is_leaf_depth and colour
-        total = total + leaf_rgb(a.color(a.child(c, j))) * (t1 - t0);
+        if (t0 < t1) {  // t0 >= 0: t_max > 0 follows
+            if (COUNT) loads += 2;  // the leaf's is_leaf_depth and colour
+            total = total + leaf_rgb(a.color(a.child(c, j))) * (t1 - t0);
+        }
     }
 }
 
@@ -1372,7 +1375,7 @@ __device__ V3 trace_df_packet(const Acc& a, V3 ro, V3 rd, bool active, uint32_t&
 }
 
 template <bool COUNT, class Acc, int LEVELS = 1>
-__global__ void __launch_bounds__(BLOCK_THREADS) df_packet_kernel(Frame f, Acc a, Outputs o, float lane_side) {
+__global__ void __launch_bounds__(BLOCK_THREADS, 5) df_packet_kernel(Frame f, Acc a, Outputs o, float lane_side) {
     __shared__ float4 s_geo[(BLOCK_THREADS / 32) * STACK_DEPTH];
     __shared__ uint2 s_ns[(BLOCK_THREADS / 32) * STACK_DEPTH];
     __shared__ uint8_t s_mask[(BLOCK_THREADS / 32) * STACK_DEPTH * 32];
