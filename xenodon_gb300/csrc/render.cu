@@ -1079,8 +1079,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS) dda_brick_kernel(Frame f, Brick
     write_outputs(f, o, ix, iy, color, loads, err);
 }
 
+// svo-rope's short dependent chains want resident warps: 12 blocks an SM.
+constexpr int svo_min_blocks(int trav) { return trav == XN_TRAV_SVO_ROPE ? 12 : 1; }
+
 template <int TRAV, bool COUNT, class Acc>
-__global__ void __launch_bounds__(BLOCK_THREADS) svo_kernel(Frame f, Acc a, Outputs o) {
+__global__ void __launch_bounds__(BLOCK_THREADS, svo_min_blocks(TRAV)) svo_kernel(Frame f, Acc a, Outputs o) {
     fill_unorm_lut();
     uint32_t ix, iy;
     if (!pixel_of_thread(f, ix, iy)) return;
