@@ -1079,11 +1079,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS) dda_brick_kernel(Frame f, Brick
     write_outputs(f, o, ix, iy, color, loads, err);
 }
 
-// svo-rope's short dependent chains want resident warps: 12 blocks an SM.
-constexpr int svo_min_blocks(int trav) { return trav == XN_TRAV_SVO_ROPE ? 12 : 1; }
-
 template <int TRAV, bool COUNT, class Acc>
-__global__ void __launch_bounds__(BLOCK_THREADS, svo_min_blocks(TRAV)) svo_kernel(Frame f, Acc a, Outputs o) {
+__device__ __forceinline__ void svo_pixel(const Frame& f, const Acc& a, const Outputs& o) {
     fill_unorm_lut();
     uint32_t ix, iy;
     if (!pixel_of_thread(f, ix, iy)) return;
@@ -1112,6 +1109,18 @@ __global__ void __launch_bounds__(BLOCK_THREADS, svo_min_blocks(TRAV)) svo_kerne
     }
     V3 color = total * voxel_emission_coeff(f, rd);
     write_outputs(f, o, ix, iy, color, loads, err);
+}
+
+template <int TRAV, bool COUNT, class Acc>
+__global__ void __launch_bounds__(BLOCK_THREADS) svo_kernel(Frame f, Acc a, Outputs o) {
+    svo_pixel<TRAV, COUNT>(f, a, o);
+}
+
+// svo-rope's steps are short dependent chains of node reads: held to 40
+// registers, twelve blocks an SM keep more of them in flight.
+template <bool COUNT, class Acc>
+__global__ void __launch_bounds__(BLOCK_THREADS, 12) svo_rope_kernel(Frame f, Acc a, Outputs o) {
+    svo_pixel<XN_TRAV_SVO_ROPE, COUNT>(f, a, o);
 }
 
 // svo-df, masked form, walked by the whole warp at once.  Each lane has its
@@ -1427,8 +1436,13 @@ __global__ void __launch_bounds__(SHARED_BLOCK) shared_stack_kernel(Frame f, Acc
 
 template <int TRAV, class Acc>
 static void launch_svo_any(bool count, const Frame& f, const Acc& a, const Outputs& o, dim3 grid, cudaStream_t s) {
-    if (count) svo_kernel<TRAV, true, Acc><<<grid, BLOCK_THREADS, 0, s>>>(f, a, o);
-    else svo_kernel<TRAV, false, Acc><<<grid, BLOCK_THREADS, 0, s>>>(f, a, o);
+    if constexpr (TRAV == XN_TRAV_SVO_ROPE) {
+        if (count) svo_rope_kernel<true, Acc><<<grid, BLOCK_THREADS, 0, s>>>(f, a, o);
+        else svo_rope_kernel<false, Acc><<<grid, BLOCK_THREADS, 0, s>>>(f, a, o);
+    } else {
+        if (count) svo_kernel<TRAV, true, Acc><<<grid, BLOCK_THREADS, 0, s>>>(f, a, o);
+        else svo_kernel<TRAV, false, Acc><<<grid, BLOCK_THREADS, 0, s>>>(f, a, o);
+    }
 }
 
 template <class Acc>
