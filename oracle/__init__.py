@@ -4,7 +4,9 @@ ctypes bindings to ``oracle/_build/liboracle.so``, the C restatement of the
 reference shaders (resources/*.comp, common.glsl, octree.glsl) and of its
 octree build (src/model/OctreeConstruction.h, Octree.cpp, Grid.cpp).  Only the
 tests, ``__graft_entry__.smoke()`` and the benchmark's CPU-baseline leg use it;
-the product library never does.
+the product library never does.  ``oracle.glsl_ref`` compiles the reference's
+own shaders for the CPU, which made the golden images that pin the
+restatement.
 """
 from __future__ import annotations
 

@@ -9,9 +9,10 @@
  * CPU baseline.  Nothing in the product (the C-ABI library, the CLI) links or
  * calls it; only tests, the smoke check and the benchmark's CPU leg do.
  *
- * Image parity for the shaders is unpinned by the reference itself (the
- * reference ships no tests, no golden images, and its Vulkan shaders cannot run
- * without a graphics stack).  The octree build is pinned by golden SVO files
+ * The restatement is pinned to the reference's own code: the shaders, compiled
+ * for the CPU from their sources by oracle/glsl_ref.py, wrote the golden images
+ * and per-ray colours of tests/golden/glsl_golden.npz, which this restatement
+ * reproduces bit for bit; the octree build is pinned by golden SVO files
  * produced by the reference's own builder compiled from its sources.
  */
 #ifndef XO_H

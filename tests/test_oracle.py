@@ -197,3 +197,43 @@ def test_oracle_counts_reference_loads(oracle_lib):
     nodes, _ = oracle_lib.build_svo(g, "sparse")
     r = oracle_lib.render("svo-naive", nodes=nodes, camera=cam, view=view)
     assert r["loads"][8, 8] % 2 == 0 and r["loads"][8, 8] >= 2
+
+
+def test_oracle_matches_the_reference_shaders(oracle_lib, glsl_golden):
+    # tests/golden/glsl_golden.npz holds what the reference's own shaders
+    # (resources/*.comp compiled for the CPU by oracle/glsl_ref.py) render for
+    # 98 cases: five traversals, six volumes (blobs, a non-cubic CT shell, a
+    # DAG and a sparse tree, a leaf root, a depth-one tree), cameras outside,
+    # inside and grazing the volume, one region of a larger display with an
+    # anisotropic voxel ratio, and every 16th row of the 128^3 blob
+    # configuration at 512x512.  The oracle's FP32 restatement must give the
+    # same RGBA8 pixels and the same float colour on every ray.
+    assert len(glsl_golden.cases) == 98
+    for case in glsl_golden.cases:
+        v = glsl_golden.view(case)
+        dda = case["traversal"] == "dda"
+        view = oracle_lib.make_view(v["width"], v["height"], v["emission"], v["ratio"], v["out_off"], v["out_ext"],
+                                    v["disp_off"], v["disp_ext"])
+        ref = oracle_lib.render(case["traversal"], grid=glsl_golden.grid(case) if dda else None,
+                                nodes=None if dda else glsl_golden.nodes(case),
+                                camera=oracle_lib.make_camera(*case["camera"]), view=view, want_loads=False)
+        rgba, colour = glsl_golden.expected(case)
+        assert np.array_equal(ref["rgba"], rgba), case["id"]
+        assert np.array_equal(ref["emission"].view(np.uint32), colour.view(np.uint32)), case["id"]
+
+
+def test_reference_shader_recipe_rewrites(tmp_path):
+    # the four rewrites oracle/glsl_ref.py makes on the way to the compiler,
+    # on a stand-in shader
+    import oracle.glsl_ref as glsl
+    (tmp_path / "inc.glsl").write_text("struct Node { uint c[8]; };\nlayout(binding = 2) readonly buffer Octree {\n"
+                                       "    Node nodes[];\n} model;\n")
+    (tmp_path / "s.comp").write_text('#version 450\n#include "inc.glsl"\n#include "inc.glsl"\n'
+                                     "uint find(vec3 pos, out vec3 base, out float side) { return 0; }\n"
+                                     "// without out-of-bounds reads\n")
+    src = glsl.shader_source(tmp_path, "s.comp")
+    assert "#version" not in src and "#include" not in src
+    assert src.count("struct Node") == 1
+    assert "Node* nodes;" in src
+    assert "uint find(vec3 pos, vec3& base, float& side)" in src
+    assert "// without out-of-bounds reads" in src
