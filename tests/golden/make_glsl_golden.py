@@ -50,6 +50,7 @@ VOLUMES = {
     "ct61x45x50": ("ct_shell", dict(dx=61, dy=45, dz=50, seed=1, device="cpu")),
     "random32": ("random_grid", dict(dx=32, dy=32, dz=32, seed=9, density=0.4, levels=3)),
     "blobs128": ("blobs", dict(n=128, seed=0)),
+    "ct512": ("ct_shell", dict(dx=512, dy=361, dz=512, seed=1, device="cpu")),
     "leaf1": ("constant", dict(shape=(1, 1, 1), rgba=(200, 100, 50, 255))),
     "two2": ("two_voxels", dict()),
 }
@@ -74,31 +75,43 @@ def sha(a: np.ndarray) -> str:
 
 
 def cases():
-    """(case id, volume id, tree type, traversal, camera id, view keywords)."""
+    """(case id, volume id, tree type, traversal, camera, view keywords)."""
+    from xenodon_gb300 import cameras
     out = []
     for cam in ("front", "oblique", "inside", "grazing"):
         for t in TRAV:
-            out.append((f"blobs32-{cam}-{t}", "blobs32", "rope", t, cam, dict(width=48, height=40)))
+            out.append((f"blobs32-{cam}-{t}", "blobs32", "rope", t, CAMS[cam], dict(width=48, height=40)))
     for cam in ("ct", "oblique", "inside"):
         for t in TRAV:
-            out.append((f"ct-{cam}-{t}", "ct61x45x50", "rope", t, cam, dict(width=40, height=32)))
+            out.append((f"ct-{cam}-{t}", "ct61x45x50", "rope", t, CAMS[cam], dict(width=40, height=32)))
     # one region of a larger display, with an anisotropic voxel ratio
     for t in TRAV:
-        out.append((f"ct-region-{t}", "ct61x45x50", "rope", t, "ct",
+        out.append((f"ct-region-{t}", "ct61x45x50", "rope", t, CAMS["ct"],
                     dict(width=0, height=0, ratio=(1.0, 1.5, 0.75), out_off=(40, 16), out_ext=(50, 37),
                          disp_off=(0, 0), disp_ext=(128, 72), emission=7.0)))
     for t in ("svo-naive", "esvo", "svo-df"):
-        out.append((f"dag-oblique-{t}", "random32", "dag", t, "oblique", dict(width=40, height=32, emission=5.0)))
-        out.append((f"sparse-grazing-{t}", "random32", "sparse", t, "grazing", dict(width=40, height=32)))
+        out.append((f"dag-oblique-{t}", "random32", "dag", t, CAMS["oblique"], dict(width=40, height=32, emission=5.0)))
+        out.append((f"sparse-grazing-{t}", "random32", "sparse", t, CAMS["grazing"], dict(width=40, height=32)))
     for vid in ("leaf1", "two2"):
         for cam in ("front", "inside"):
             for t in TRAV:
-                out.append((f"{vid}-{cam}-{t}", vid, "rope", t, cam, dict(width=24, height=20)))
+                out.append((f"{vid}-{cam}-{t}", vid, "rope", t, CAMS[cam], dict(width=24, height=20)))
     # the 128^3 blob configuration at 512x512, every 16th row
     for row in range(0, 512, 16):
-        out.append((f"c0-row{row:03d}-dda", "blobs128", None, "dda", "c0",
+        out.append((f"c0-row{row:03d}-dda", "blobs128", None, "dda", CAMS["c0"],
                     dict(width=0, height=0, out_off=(0, row), out_ext=(512, 1), disp_off=(0, 0),
                          disp_ext=(512, 512))))
+    # the 512x361x512 CT configuration at 1920x1080: a frame from each leg of
+    # its path (orbit 37, dolly 220, rotation about an interior point 330 and
+    # 440), two rows each, every traversal
+    path = cameras.ct_path()
+    for frame in (37, 220, 330, 440):
+        cam = tuple(tuple(float(x) for x in v) for v in path[frame])
+        for row in (11 + frame % 7, 540 + frame % 13):
+            for t in TRAV:
+                out.append((f"c1-f{frame}-row{row:04d}-{t}", "ct512", "rope", t, cam,
+                            dict(width=0, height=0, out_off=(0, row), out_ext=(1920, 1), disp_off=(0, 0),
+                                 disp_ext=(1920, 1080))))
     return out
 
 
@@ -111,22 +124,24 @@ def view_args(kw):
 def main() -> None:
     if not glsl.build():
         raise SystemExit("set XENODON_REFERENCE to the reference checkout")
-    grids, trees, meta, arrays = {}, {}, [], {}
+    grids, trees, hashes, meta, arrays = {}, {}, {}, [], {}
     for cid, vid, typ, trav, cam, kw in cases():
         if vid not in grids:
             grids[vid] = make_volume(vid)
+            hashes[vid] = sha(grids[vid])
         grid = grids[vid]
         nodes = None
         if trav != "dda":
             if (vid, typ) not in trees:
                 trees[(vid, typ)] = oracle.build_svo(grid, typ)[0]
+                hashes[(vid, typ)] = sha(trees[(vid, typ)])
             nodes = trees[(vid, typ)]
-        rgba, colour = glsl.render(trav, CAMS[cam], kw["width"], kw["height"], grid=grid if trav == "dda" else None,
+        rgba, colour = glsl.render(trav, cam, kw["width"], kw["height"], grid=grid if trav == "dda" else None,
                                    nodes=nodes, **view_args(kw))
         arrays[f"{cid}/rgba"] = rgba
         arrays[f"{cid}/colour"] = colour
-        meta.append(dict(id=cid, volume=vid, tree=typ, traversal=trav, camera=CAMS[cam], view=kw,
-                         grid_sha256=sha(grid), nodes_sha256=None if nodes is None else sha(nodes)))
+        meta.append(dict(id=cid, volume=vid, tree=typ, traversal=trav, camera=cam, view=kw,
+                         grid_sha256=hashes[vid], nodes_sha256=None if nodes is None else hashes[(vid, typ)]))
     arrays["cases"] = np.frombuffer(json.dumps(dict(volumes=VOLUMES, cases=meta)).encode(), np.uint8)
     np.savez_compressed(OUT, **arrays)
     print(f"{len(meta)} cases -> {OUT} ({OUT.stat().st_size} bytes)")

@@ -214,16 +214,25 @@ def test_c3_lean_octree_equals_full_build_on_1024_field(ctx):
 
 
 def test_cuda_matches_the_reference_shaders(ctx, glsl_golden):
-    # the 98 cases of tests/golden/glsl_golden.npz, rendered by the reference's
-    # own shaders compiled for the CPU (five traversals; blobs, a non-cubic CT
-    # shell, DAG and sparse trees, a leaf root, a depth-one tree; cameras
-    # outside, inside and grazing; a display region with an anisotropic voxel
-    # ratio; every 16th row of the 128^3 blob configuration at 512x512): the
-    # CUDA kernels give the same RGBA8 pixels and the same float colour on
-    # every ray
+    # the 138 cases of tests/golden/glsl_golden.npz, rendered by the
+    # reference's own shaders compiled for the CPU (five traversals; blobs, a
+    # non-cubic CT shell, DAG and sparse trees, a leaf root, a depth-one tree;
+    # cameras outside, inside and grazing; a display region with an
+    # anisotropic voxel ratio; every 16th row of the 128^3 blob configuration
+    # at 512x512; rows of a frame from each leg of the 512x361x512 CT
+    # configuration's path at 1920x1080): the CUDA kernels give the same
+    # RGBA8 pixels and the same float colour on every ray.  A case whose
+    # volume this host does not regenerate byte for byte is left out: the
+    # full-size CT volume, whose generator rounds a few voxels differently on
+    # some hosts; there its frames are checked against the oracle
+    # (test_c1_ct_path_legs), which the CPU tests pin to these rows.
     import xenodon_gb300 as xg
     vols = {}
+    left_out = {c["volume"] for c in glsl_golden.cases if not glsl_golden.reproducible(c)}
+    assert left_out <= {"ct512"}, left_out
     for case in glsl_golden.cases:
+        if case["volume"] in left_out:
+            continue
         v = glsl_golden.view(case)
         trav = case["traversal"]
         key = (case["volume"], "grid" if trav == "dda" else case["tree"])

@@ -202,13 +202,15 @@ def test_oracle_counts_reference_loads(oracle_lib):
 def test_oracle_matches_the_reference_shaders(oracle_lib, glsl_golden):
     # tests/golden/glsl_golden.npz holds what the reference's own shaders
     # (resources/*.comp compiled for the CPU by oracle/glsl_ref.py) render for
-    # 98 cases: five traversals, six volumes (blobs, a non-cubic CT shell, a
-    # DAG and a sparse tree, a leaf root, a depth-one tree), cameras outside,
-    # inside and grazing the volume, one region of a larger display with an
-    # anisotropic voxel ratio, and every 16th row of the 128^3 blob
-    # configuration at 512x512.  The oracle's FP32 restatement must give the
-    # same RGBA8 pixels and the same float colour on every ray.
-    assert len(glsl_golden.cases) == 98
+    # 138 cases: five traversals, six small volumes (blobs, a non-cubic CT
+    # shell, a DAG and a sparse tree, a leaf root, a depth-one tree), cameras
+    # outside, inside and grazing the volume, one region of a larger display
+    # with an anisotropic voxel ratio, every 16th row of the 128^3 blob
+    # configuration at 512x512, and two rows of a frame from each leg of the
+    # 512x361x512 CT configuration's path at 1920x1080.  The oracle's FP32
+    # restatement must give the same RGBA8 pixels and the same float colour
+    # on every ray.
+    assert len(glsl_golden.cases) == 138
     for case in glsl_golden.cases:
         v = glsl_golden.view(case)
         dda = case["traversal"] == "dda"
