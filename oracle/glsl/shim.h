@@ -10,9 +10,13 @@
 // `T name[];` written `T* name;`.  The GLSL qualifiers and block names become
 // the C++ declarations below.
 //
-// The built-ins follow their definitions in the GLSL 4.50 specification, in
-// IEEE single precision without contraction (the recipe passes
-// -ffp-contract=off): min(x, y) = y < x ? y : x, max(x, y) = x < y ? y : x,
+// Arithmetic is IEEE single precision, every operation (division and sqrt
+// included) correctly rounded and none contracted (the recipe passes
+// -ffp-contract=off); GLSL allows less exact division and square roots, and
+// a GPU driver may fuse a multiply and an add, so this is one admissible
+// evaluation of the shaders, the one the restatement and the CUDA kernels
+// follow.  The built-ins follow their definitions in the GLSL 4.50
+// specification: min(x, y) = y < x ? y : x, max(x, y) = x < y ? y : x,
 // mod(x, y) = x - y * floor(x / y), length(x) = sqrt(dot(x, x)),
 // normalize(x) = x / length(x), dot summed from the first component, cross as
 // defined there, sign(x) in {-1, 0, 1}.  unpackUnorm4x8 and texelFetch of an
