@@ -7,7 +7,7 @@
 // header, with four mechanical rewrites and nothing else changed: the
 // `#version` line dropped, `#include "*.glsl"` replaced by the file, an `out T
 // name` parameter written `T& name`, and a buffer block's unsized array
-// `T name[];` written `T* name;`.  The GLSL qualifiers and block names become
+// `T name[];` written `XoBuffer<T> name;`.  The GLSL qualifiers and block names become
 // the C++ declarations below.
 //
 // Arithmetic is IEEE single precision, every operation (division and sqrt
@@ -302,12 +302,28 @@ inline vec4 unpackUnorm4x8(uint c) {
 
 // --------------------------------------------------- resources of a pass ---
 
+// Words the current invocation has read from the model: texels fetched and
+// node buffer accesses.  In these shaders every `model.nodes[i]` expression
+// is followed by one field (`children[k]`, `color` or `is_leaf_depth`), so
+// each access of the buffer reads one 32-bit word.
+static uint64_t xo_words_read;
+
+// The node buffer's unsized array, written `XoBuffer<T> name;` by the recipe.
+template <class T> struct XoBuffer {
+    const T* p = nullptr;
+    const T& operator[](uint64_t i) const {
+        ++xo_words_read;
+        return p[i];
+    }
+};
+
 // An RGBA8 3D texture, x fastest, read with texelFetch.
 struct sampler3D {
     const uint8_t* rgba = nullptr;
     int dx = 0, dy = 0, dz = 0;
 };
 inline vec4 texelFetch(const sampler3D& s, const ivec3& p, int) {
+    ++xo_words_read;
     if (p.x < 0 || p.y < 0 || p.z < 0 || p.x >= s.dx || p.y >= s.dy || p.z >= s.dz) return vec4(0);
     const uint8_t* t = s.rgba + 4 * ((size_t)p.x + (size_t)s.dx * ((size_t)p.y + (size_t)s.dy * (size_t)p.z));
     return vec4(float(t[0]) / 255.0f, float(t[1]) / 255.0f, float(t[2]) / 255.0f, float(t[3]) / 255.0f);

@@ -13,7 +13,8 @@ the way the text gets four mechanical rewrites, and no other change:
 * an ``out T name`` parameter becomes ``T& name`` (GLSL copies an out
   parameter back on return; every such parameter in these shaders is only
   written, immediately before a return, so a reference is the same);
-* a buffer block's unsized array ``T name[];`` becomes ``T* name;``.
+* a buffer block's unsized array ``T name[];`` becomes ``XoBuffer<T> name;``
+  (an array view that counts its accesses: the words the shader reads).
 
 The libraries run the shader's ``main`` once per pixel, with the push
 constants and uniforms the reference's host code sets.  They make golden
@@ -67,7 +68,7 @@ def shader_source(resources: Path, name: str, _seen: set | None = None) -> str:
                 out.append(shader_source(resources, inc, seen))
             continue
         line = _OUT_PARAM.sub(r"\1& \2", line)
-        line = _UNSIZED.sub(r"\1\2* \3;", line)
+        line = _UNSIZED.sub(r"\1XoBuffer<\2> \3;", line)
         out.append(line)
     return "\n".join(out)
 
@@ -107,7 +108,8 @@ def _lib(trav: str):
         fn = lib.xo_glsl_render
         fn.restype = ctypes.c_int
         fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
-                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p]
+                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p,
+                       ctypes.c_void_p]
         _libs[trav] = (lib, fn)
     return _libs[trav][1]
 
@@ -118,7 +120,8 @@ def render(trav: str, camera, width: int, height: int, emission: float = 10.0, r
     """Run the reference shader `trav` over an output region.  camera:
     (forward, up, translation); grid: (dz, dy, dx, 4) uint8 for dda; nodes:
     (n, 10) uint32 for the octree shaders.  Returns (rgba (h, w, 4) uint8,
-    colour (h, w, 3) float32: the colour handed to imageStore)."""
+    colour (h, w, 3) float32: the colour handed to imageStore, words (h, w)
+    uint32: the words each invocation read from the model)."""
     out_ext = out_ext or (width, height)
     disp_ext = disp_ext or (width, height)
     w, h = out_ext
@@ -136,6 +139,7 @@ def render(trav: str, camera, width: int, height: int, emission: float = 10.0, r
         gp, npn = None, nd.ctypes.data
     colour = np.zeros((h, w, 4), np.float32)
     rgba = np.zeros((h, w, 4), np.uint8)
+    words = np.zeros((h, w), np.uint32)
     _lib(trav)(gp, dims.ctypes.data, npn, cam.ctypes.data, region.ctypes.data, extent.ctypes.data,
-               rat.ctypes.data, float(emission), colour.ctypes.data, rgba.ctypes.data)
-    return rgba, colour[..., :3].copy()
+               rat.ctypes.data, float(emission), colour.ctypes.data, rgba.ctypes.data, words.ctypes.data)
+    return rgba, colour[..., :3].copy(), words

@@ -104,7 +104,8 @@ class GlslGolden:
         return self.tree(case)[0]
 
     def expected(self, case):
-        return self.z[case["id"] + "/rgba"], self.z[case["id"] + "/colour"]
+        """RGBA8 image, float colour and words read per ray."""
+        return self.z[case["id"] + "/rgba"], self.z[case["id"] + "/colour"], self.z[case["id"] + "/words"]
 
     @staticmethod
     def view(case):

@@ -5,7 +5,9 @@ The shaders (resources/dda.comp, svo_naive.comp, esvo.comp, svo_df.comp,
 svo_rope.comp with common.glsl and octree.glsl) are compiled for the CPU by
 ``oracle/glsl_ref.py`` and run once per pixel.  Each case stores the RGBA8
 image and the float colour the shader hands to imageStore (after the emission
-coefficient, before the RGBA8 conversion).  The volumes come from the
+coefficient, before the RGBA8 conversion) and the 32-bit words each ray read
+from the model (texels or node words: the roofline's algorithmic bytes / 4).
+The volumes come from the
 deterministic generators in ``xenodon_gb300.volumes`` and the octrees from the
 oracle's builder (itself pinned byte for byte to the reference's builder by
 svo_golden.npz); their SHA-256 is stored so that a test notices a generator
@@ -136,10 +138,11 @@ def main() -> None:
                 trees[(vid, typ)] = oracle.build_svo(grid, typ)[0]
                 hashes[(vid, typ)] = sha(trees[(vid, typ)])
             nodes = trees[(vid, typ)]
-        rgba, colour = glsl.render(trav, cam, kw["width"], kw["height"], grid=grid if trav == "dda" else None,
-                                   nodes=nodes, **view_args(kw))
+        rgba, colour, words = glsl.render(trav, cam, kw["width"], kw["height"], grid=grid if trav == "dda" else None,
+                                          nodes=nodes, **view_args(kw))
         arrays[f"{cid}/rgba"] = rgba
         arrays[f"{cid}/colour"] = colour
+        arrays[f"{cid}/words"] = words
         meta.append(dict(id=cid, volume=vid, tree=typ, traversal=trav, camera=cam, view=kw,
                          grid_sha256=hashes[vid], nodes_sha256=None if nodes is None else hashes[(vid, typ)]))
     arrays["cases"] = np.frombuffer(json.dumps(dict(volumes=VOLUMES, cases=meta)).encode(), np.uint8)

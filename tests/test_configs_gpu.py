@@ -221,7 +221,8 @@ def test_cuda_matches_the_reference_shaders(ctx, glsl_golden):
     # anisotropic voxel ratio; every 16th row of the 128^3 blob configuration
     # at 512x512; rows of a frame from each leg of the 512x361x512 CT
     # configuration's path at 1920x1080): the CUDA kernels give the same
-    # RGBA8 pixels and the same float colour on every ray.  A case whose
+    # RGBA8 pixels, the same float colour and the same count of words read
+    # from the model on every ray.  A case whose
     # volume this host does not regenerate byte for byte is left out: the
     # full-size CT volume, whose generator rounds a few voxels differently on
     # some hosts; there its frames are checked against the oracle
@@ -244,9 +245,10 @@ def test_cuda_matches_the_reference_shaders(ctx, glsl_golden):
                 vols[key] = ctx.upload_svo(nodes, side)
         p = xg.make_params(v["width"], v["height"], v["emission"], v["ratio"], v["out_off"], v["out_ext"],
                            v["disp_off"], v["disp_ext"])
-        rgba, em, _ = ctx.render(vols[key], trav, xg.make_camera(*case["camera"]), p, emission=True)
-        want_rgba, want_colour = glsl_golden.expected(case)
+        rgba, em, words = _device_render(ctx, vols[key], trav, xg.make_camera(*case["camera"]), p)
+        want_rgba, want_colour, want_words = glsl_golden.expected(case)
         assert np.array_equal(rgba, want_rgba), case["id"]
         assert np.array_equal(em.view(np.uint32), want_colour.view(np.uint32)), case["id"]
+        assert np.array_equal(words, want_words), case["id"]
     for vol in vols.values():
         vol.release()

@@ -208,8 +208,8 @@ def test_oracle_matches_the_reference_shaders(oracle_lib, glsl_golden):
     # with an anisotropic voxel ratio, every 16th row of the 128^3 blob
     # configuration at 512x512, and two rows of a frame from each leg of the
     # 512x361x512 CT configuration's path at 1920x1080.  The oracle's FP32
-    # restatement must give the same RGBA8 pixels and the same float colour
-    # on every ray.
+    # restatement must give the same RGBA8 pixels, the same float colour and
+    # the same count of words read from the model on every ray.
     assert len(glsl_golden.cases) == 138
     for case in glsl_golden.cases:
         v = glsl_golden.view(case)
@@ -218,10 +218,11 @@ def test_oracle_matches_the_reference_shaders(oracle_lib, glsl_golden):
                                     v["disp_off"], v["disp_ext"])
         ref = oracle_lib.render(case["traversal"], grid=glsl_golden.grid(case) if dda else None,
                                 nodes=None if dda else glsl_golden.nodes(case),
-                                camera=oracle_lib.make_camera(*case["camera"]), view=view, want_loads=False)
-        rgba, colour = glsl_golden.expected(case)
+                                camera=oracle_lib.make_camera(*case["camera"]), view=view)
+        rgba, colour, words = glsl_golden.expected(case)
         assert np.array_equal(ref["rgba"], rgba), case["id"]
         assert np.array_equal(ref["emission"].view(np.uint32), colour.view(np.uint32)), case["id"]
+        assert np.array_equal(ref["loads"], words), case["id"]
 
 
 def test_reference_shader_recipe_rewrites(tmp_path):
@@ -236,7 +237,7 @@ def test_reference_shader_recipe_rewrites(tmp_path):
     src = glsl.shader_source(tmp_path, "s.comp")
     assert "#version" not in src and "#include" not in src
     assert src.count("struct Node") == 1
-    assert "Node* nodes;" in src
+    assert "XoBuffer<Node> nodes;" in src
     assert "uint find(vec3 pos, vec3& base, float& side)" in src
     assert "// without out-of-bounds reads" in src
 
@@ -245,8 +246,8 @@ def test_oracle_matches_the_reference_shaders_random(oracle_lib):
     # the reference's shaders themselves (oracle/glsl_ref.py), where the
     # reference checkout is present, against the restatement on random grids
     # (1 to 47 texels a side), all three tree types, random voxel ratios and
-    # cameras anywhere around or inside the volume: identical pixels and
-    # float colours on every ray
+    # cameras anywhere around or inside the volume: identical pixels, float
+    # colours and word counts on every ray
     import oracle.glsl_ref as glsl
     if glsl.reference_dir() is not None:
         glsl.build()
@@ -271,9 +272,10 @@ def test_oracle_matches_the_reference_shaders_random(oracle_lib):
             if trav == "svo-rope" and tree != "rope":
                 continue
             dda = trav == "dda"
-            rgba, colour = glsl.render(trav, cam, 24, 20, emission=5.0, ratio=ratio, grid=g if dda else None,
-                                       nodes=None if dda else nodes)
+            rgba, colour, words = glsl.render(trav, cam, 24, 20, emission=5.0, ratio=ratio, grid=g if dda else None,
+                                              nodes=None if dda else nodes)
             ref = oracle_lib.render(trav, grid=g if dda else None, nodes=None if dda else nodes,
-                                    camera=oracle_lib.make_camera(*cam), view=view, want_loads=False)
+                                    camera=oracle_lib.make_camera(*cam), view=view)
             assert np.array_equal(ref["rgba"], rgba), (i, trav)
             assert np.array_equal(ref["emission"].view(np.uint32), colour.view(np.uint32)), (i, trav)
+            assert np.array_equal(ref["loads"], words), (i, trav)
