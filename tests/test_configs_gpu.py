@@ -252,3 +252,70 @@ def test_cuda_matches_the_reference_shaders(ctx, glsl_golden):
         assert np.array_equal(words, want_words), case["id"]
     for vol in vols.values():
         vol.release()
+
+
+def _golden_cases(glsl_golden):
+    left_out = {c["volume"] for c in glsl_golden.cases if not glsl_golden.reproducible(c)}
+    assert left_out <= {"ct512"}, left_out
+    return [c for c in glsl_golden.cases if c["volume"] not in left_out]
+
+
+def test_batch_matches_the_reference_shaders(ctx, glsl_golden):
+    # the golden cases (as above) as one batch: the persistent batch kernel,
+    # one launch over every case's warp tiles, gives the reference shaders'
+    # RGBA8 pixels
+    import torch
+    import xenodon_gb300 as xg
+    cases = _golden_cases(glsl_golden)
+    vols, specs, bufs = {}, [], []
+    for case in cases:
+        v = glsl_golden.view(case)
+        trav = case["traversal"]
+        key = (case["volume"], "grid" if trav == "dda" else case["tree"])
+        if key not in vols:
+            if trav == "dda":
+                vols[key] = ctx.upload_grid(glsl_golden.grid(case))
+            else:
+                nodes, side = glsl_golden.tree(case)
+                vols[key] = ctx.upload_svo(nodes, side)
+        p = xg.make_params(v["width"], v["height"], v["emission"], v["ratio"], v["out_off"], v["out_ext"],
+                           v["disp_off"], v["disp_ext"])
+        buf = torch.zeros((p.output_region.height, p.output_region.width), dtype=torch.int32, device="cuda")
+        specs.append((vols[key], trav, xg.make_camera(*case["camera"]), p, buf.data_ptr()))
+        bufs.append(buf)
+    jobs = ctx.make_jobs(specs)
+    ctx.render_batch(jobs, len(specs), xg.BatchConfig(8, 128, 0, 1), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    for case, buf in zip(cases, bufs):
+        img = buf.cpu().numpy().view(np.uint8).reshape(buf.shape[0], buf.shape[1], 4)
+        assert np.array_equal(img, glsl_golden.expected(case)[0]), case["id"]
+    for vol in vols.values():
+        vol.release()
+
+
+def test_server_matches_the_reference_shaders(ctx, glsl_golden):
+    # the golden cases (as above) submitted to the render server at once: the
+    # small frames fold into its running persistent kernel; every result is
+    # the reference shaders' RGBA8 image
+    import xenodon_gb300 as xg
+    cases = _golden_cases(glsl_golden)
+    ids = {}
+    with xg.Server(ctx, max_batch_jobs=64, streams=2) as server:
+        tickets = []
+        for case in cases:
+            v = glsl_golden.view(case)
+            trav = case["traversal"]
+            key = (case["volume"], "grid" if trav == "dda" else case["tree"])
+            if key not in ids:
+                ids[key] = len(ids) + 1
+                if trav == "dda":
+                    server.add_grid(ids[key], glsl_golden.grid(case))
+                else:
+                    nodes, side = glsl_golden.tree(case)
+                    server.add_svo(ids[key], nodes, side)
+            p = xg.make_params(v["width"], v["height"], v["emission"], v["ratio"], v["out_off"], v["out_ext"],
+                               v["disp_off"], v["disp_ext"])
+            tickets.append(server.submit(ids[key], trav, xg.make_camera(*case["camera"]), p))
+        for case, t in zip(cases, tickets):
+            rgba, _ = server.wait(t, timeout=60)
+            assert np.array_equal(rgba, glsl_golden.expected(case)[0]), case["id"]
