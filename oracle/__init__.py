@@ -20,6 +20,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "liboracle.so"
 REF_BUILDER = HERE / "_ref" / "xn_ref_build"
+REF_CONFIG = HERE / "_ref" / "xn_ref_config"
 
 TRAVERSALS = {"dda": 0, "svo-naive": 1, "esvo": 2, "svo-df": 3, "svo-rope": 4}
 TYPES = {"sparse": 0, "dag": 1, "rope": 2}
@@ -65,6 +66,18 @@ def build_ref() -> bool:
     if not ref or not (Path(ref) / "src" / "model" / "OctreeConstruction.h").exists():
         return REF_BUILDER.exists()
     subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REFERENCE={ref}"], check=True)
+    return True
+
+
+def build_ref_config() -> bool:
+    """Compile the reference's own headless.conf parser (src/core/Parser.cpp,
+    Config.h, src/backend/headless/HeadlessConfig.cpp) from the checkout that
+    XENODON_REFERENCE names; without one, report whether it was compiled
+    before."""
+    ref = os.environ.get("XENODON_REFERENCE", "")
+    if not ref or not (Path(ref) / "src" / "core" / "Parser.cpp").exists():
+        return REF_CONFIG.exists()
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref-config", f"REFERENCE={ref}"], check=True)
     return True
 
 

@@ -109,3 +109,86 @@ def test_help_and_unknown_subcommand(built_library):
     assert rc == 1 and "Error: No such topic nope" in out
     rc, out = run("bogus")
     assert rc == 1 and "Error: Invalid subcommand 'bogus'" in out
+
+
+_CONF_DRIVER = r'''
+#include <cstdio>
+#include <fstream>
+#include <sstream>
+#include "cli_util.h"
+// prints what the command line's headless.conf parser makes of a file, in the
+// form of oracle/ref_config_driver.cpp
+int main(int argc, char** argv) {
+    std::ifstream in(argv[1], std::ios::binary);
+    std::stringstream ss;
+    ss << in.rdbuf();
+    try {
+        for (const auto& d : cli::parse_headless_config(ss.str()))
+            std::printf("device %u %d %d %u %u\n", (unsigned)d.vkindex, d.region.x, d.region.y, d.region.width,
+                        d.region.height);
+    } catch (const cli::Error& e) {
+        std::string m = e.what();
+        std::printf("error: ");
+        std::fwrite(m.data(), 1, m.size(), stdout);
+        std::printf("\n");
+    }
+    return 0;
+}
+'''
+
+
+def test_headless_conf_parser_matches_the_reference(tmp_path):
+    # the reference's own parser (src/core/Parser.cpp, Config.h,
+    # src/backend/headless/HeadlessConfig.cpp, compiled by `make -C oracle
+    # ref-config`) and the command line's, on edge cases and 1500 random
+    # mutations of valid files: the same devices, or the same error message
+    import random
+    from pathlib import Path
+    import oracle
+    if not oracle.build_ref_config():
+        pytest.skip("reference sources not present")
+    root = Path(__file__).resolve().parents[1]
+    drv = tmp_path / "conf.cpp"
+    drv.write_text(_CONF_DRIVER)
+    ours = tmp_path / "conf"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", str(root / "xenodon_gb300" / "host"), "-I",
+                    str(root / "include"), str(drv), str(root / "xenodon_gb300" / "host" / "cli_util.cpp"), "-o",
+                    str(ours)], check=True)
+    valid = [
+        "device {\n  vkindex = 0\n  offset = (0, 0)\n  extent = (512, 512)\n}\n",
+        "device { vkindex = 0 offset = (0, 0) extent = (960, 1080) }\n"
+        "device { vkindex = 1 offset = (960, 0) extent = (960, 1080) }\n",
+        "# a comment\ndevice {\n\tvkindex = 3\n\textent = (17, 4)\n\toffset = (5, 6)\n}\n# trailing\n",
+        "device{vkindex=0 offset=(1,2) extent=(3,4)}",
+        "device {\n  vkindex = 0\n  offset = ( 0 , 0 )\n  extent = ( 512 , 512 )\n}\n\n\n",
+    ]
+    cases = valid + [
+        "", "\n", "device {}", "device { vkindex = 0 }", "Device { }", "8device{}",
+        "device { vkindex = 99999999999999999999 offset = (4294967296, 2147483648) extent = (4294967297, 0) }",
+        "device { vkindex = 0 offset = (0, 0) extent = (1, 1) } x",
+        "device { vkindex = 0 vkindex = 1 offset = (0,0) extent=(1,1) }",
+        "device { vkindex = 0 offset = (0, 0) extent = (1, 1) }#c",
+        "device { vkindex = 0 offset = (0, 0) extent = (1, 1) \n",
+        "device\n{ vkindex = 0 offset = (0,0) extent=(1,1) }",
+        "device { vkindex = 0\n offset = (0, 0)\nvkindex  extent = (1, 1) }",
+    ]
+    alphabet = list("{}()=,#\n \t\r0123456789abcdevkinxofsetrzq\"\\-+") + ["device", "vkindex", "offset", "extent"]
+    rng = random.Random(5)
+    for _ in range(1500):
+        s = list(rng.choice(valid))
+        for _ in range(rng.randint(1, 6)):
+            i = rng.randint(0, len(s))
+            op = rng.random()
+            if op < 0.35 and s:
+                del s[min(i, len(s) - 1)]
+            elif op < 0.7:
+                s.insert(i, rng.choice(alphabet))
+            elif s:
+                s[min(i, len(s) - 1)] = rng.choice(alphabet)
+        cases.append("".join(s))
+    f = tmp_path / "c.conf"
+    for c in cases:
+        f.write_bytes(c.encode())
+        ref = subprocess.run([str(oracle.REF_CONFIG), str(f)], capture_output=True, timeout=30).stdout
+        got = subprocess.run([str(ours), str(f)], capture_output=True, timeout=30).stdout
+        assert got == ref, (c, ref, got)

@@ -191,33 +191,44 @@ std::vector<HeadlessDevice> parse_headless_config(const std::string& text) {
         parse_items(p, [&](const std::string& kk) {
             bool* seen = kk == "vkindex" ? &have_index : kk == "offset" ? &have_offset : kk == "extent" ? &have_extent : nullptr;
             if (!seen) return false;
-            if (*seen) throw Error("Configuration error: Ambiguous key '" + kk + "'");
-            *seen = true;
+            // the value is parsed before a repeated key is refused
+            // (src/core/Config.h: accum(item.key, item.parse(*this)))
             p.expect('=');
             p.optws();
+            HeadlessDevice v = d;
             if (kk == "vkindex") {
-                d.vkindex = p.number();
+                v.vkindex = p.number();
             } else if (kk == "offset") {
-                auto v = p.pair();
-                d.region.x = (int32_t)v.first;
-                d.region.y = (int32_t)v.second;
+                auto xy = p.pair();
+                v.region.x = (int32_t)xy.first;
+                v.region.y = (int32_t)xy.second;
             } else {
-                auto v = p.pair();
-                d.region.width = (uint32_t)v.first;
-                d.region.height = (uint32_t)v.second;
+                auto wh = p.pair();
+                v.region.width = (uint32_t)wh.first;
+                v.region.height = (uint32_t)wh.second;
             }
+            if (*seen) throw Error("Configuration error: Ambiguous key '" + kk + "'");
+            *seen = true;
+            d = v;
             return true;
         });
-        if (!have_index) throw Error("Configuration error: Missing key 'vkindex'");
-        if (!have_offset) throw Error("Configuration error: Missing key 'offset'");
+        // src/core/Config.h:205 builds the device from the accumulators'
+        // get() calls as the arguments of one std::tuple constructor; built
+        // with GCC those are evaluated last to first, so of several missing
+        // keys the reference reports the last (extent, offset, vkindex)
         if (!have_extent) throw Error("Configuration error: Missing key 'extent'");
+        if (!have_offset) throw Error("Configuration error: Missing key 'offset'");
+        if (!have_index) throw Error("Configuration error: Missing key 'vkindex'");
         p.expect('}');
         devices.push_back(d);
         return true;
     });
+    // src/backend/headless/HeadlessConfig.cpp:23-25 refuses an empty device
+    // list before cfg::Config::as (src/core/Config.h:144-151) looks for the
+    // end of the input
+    if (devices.empty()) throw Error("Configuration error: At least one device entry is required");
     int c = p.peek();
     if (c > 0) p.fail_at(std::string("Expected end of input, found '") + (char)c + "'");
-    if (devices.empty()) throw Error("Configuration error: At least one device entry is required");
     return devices;
 }
 
