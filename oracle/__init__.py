@@ -21,6 +21,7 @@ HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "liboracle.so"
 REF_BUILDER = HERE / "_ref" / "xn_ref_build"
 REF_CONFIG = HERE / "_ref" / "xn_ref_config"
+REF_PNG = HERE / "_ref" / "xn_ref_png"
 
 TRAVERSALS = {"dda": 0, "svo-naive": 1, "esvo": 2, "svo-df": 3, "svo-rope": 4}
 TYPES = {"sparse": 0, "dag": 1, "rope": 2}
@@ -78,6 +79,17 @@ def build_ref_config() -> bool:
     if not ref or not (Path(ref) / "src" / "core" / "Parser.cpp").exists():
         return REF_CONFIG.exists()
     subprocess.run(["make", "-s", "-C", str(HERE), "ref-config", f"REFERENCE={ref}"], check=True)
+    return True
+
+
+def build_ref_png() -> bool:
+    """Compile a decoder from the reference's PNG library (subprojects/lodepng)
+    from the checkout that XENODON_REFERENCE names; without one, report
+    whether it was compiled before."""
+    ref = os.environ.get("XENODON_REFERENCE", "")
+    if not ref or not (Path(ref) / "subprojects" / "lodepng" / "lodepng.cpp").exists():
+        return REF_PNG.exists()
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref-png", f"REFERENCE={ref}"], check=True)
     return True
 
 

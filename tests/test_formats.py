@@ -285,6 +285,35 @@ def test_png_compresses_a_rendered_frame(built_library, tmp_path):
     assert np.array_equal(_png_decode((tmp_path / "b.png").read_bytes()), blank)
 
 
+def test_png_files_decode_with_the_reference_png_library(built_library, tmp_path):
+    # the PNG library the reference writes its frames with (subprojects/lodepng,
+    # compiled by `make -C oracle ref-png`) decodes the library's PNG files,
+    # every filter and deflate path among them, to exactly their pixels
+    import subprocess
+    import oracle
+    import xenodon_gb300 as xg
+    if not oracle.build_ref_png():
+        pytest.skip("reference sources not present")
+    rng = np.random.default_rng(11)
+    h, w = 720, 1280
+    yy, xx = np.mgrid[0:h, 0:w]
+    r = np.hypot(yy - h / 2, xx - w / 2)
+    frame = np.zeros((h, w, 4), np.uint8)
+    frame[..., 3] = 255
+    frame[..., 0] = np.where(r < 250, (255 - r).clip(0, 255), 0).astype(np.uint8)
+    frame[..., 1] = np.where(r < 250, xx % 256, 0).astype(np.uint8)
+    frame[300:340, 100:400, 2] = rng.integers(0, 256, (40, 300))
+    images = [rng.integers(0, 256, s + (4,)).astype(np.uint8) for s in ((1, 1), (3, 7), (33, 47), (2, 1920))]
+    images += [frame, np.zeros((64, 4000, 4), np.uint8), np.full((17, 5, 4), 255, np.uint8)]
+    for k, img in enumerate(images):
+        f, raw = tmp_path / f"{k}.png", tmp_path / f"{k}.rgba"
+        xg.png_save(f, img)
+        out = subprocess.run([str(oracle.REF_PNG), str(f), str(raw)], capture_output=True, text=True,
+                             timeout=60).stdout
+        assert out.strip() == f"ok {img.shape[1]} {img.shape[0]}", out
+        assert np.array_equal(np.fromfile(raw, np.uint8).reshape(img.shape), img), k
+
+
 @pytest.mark.parametrize("compression", [5, 8, 32946, 32773])
 @pytest.mark.parametrize("predictor", [1, 2])
 @pytest.mark.parametrize("layout", ["strips", "tiles"])
