@@ -22,6 +22,7 @@ LIB_PATH = HERE / "_build" / "liboracle.so"
 REF_BUILDER = HERE / "_ref" / "xn_ref_build"
 REF_CONFIG = HERE / "_ref" / "xn_ref_config"
 REF_PNG = HERE / "_ref" / "xn_ref_png"
+REF_RECT = HERE / "_ref" / "xn_ref_rect"
 
 TRAVERSALS = {"dda": 0, "svo-naive": 1, "esvo": 2, "svo-df": 3, "svo-rope": 4}
 TYPES = {"sparse": 0, "dag": 1, "rope": 2}
@@ -90,6 +91,17 @@ def build_ref_png() -> bool:
     if not ref or not (Path(ref) / "subprojects" / "lodepng" / "lodepng.cpp").exists():
         return REF_PNG.exists()
     subprocess.run(["make", "-s", "-C", str(HERE), "ref-png", f"REFERENCE={ref}"], check=True)
+    return True
+
+
+def build_ref_rect() -> bool:
+    """Compile the reference's own rect_union (src/utility/rect_union.h) behind
+    a driver, from the checkout that XENODON_REFERENCE names; without one,
+    report whether it was compiled before."""
+    ref = os.environ.get("XENODON_REFERENCE", "")
+    if not ref or not (Path(ref) / "src" / "utility" / "rect_union.h").exists():
+        return REF_RECT.exists()
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref-rect", f"REFERENCE={ref}"], check=True)
     return True
 
 
