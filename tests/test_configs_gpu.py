@@ -222,18 +222,10 @@ def test_cuda_matches_the_reference_shaders(ctx, glsl_golden):
     # at 512x512; rows of a frame from each leg of the 512x361x512 CT
     # configuration's path at 1920x1080): the CUDA kernels give the same
     # RGBA8 pixels, the same float colour and the same count of words read
-    # from the model on every ray.  A case whose
-    # volume this host does not regenerate byte for byte is left out: the
-    # full-size CT volume, whose generator rounds a few voxels differently on
-    # some hosts; there its frames are checked against the oracle
-    # (test_c1_ct_path_legs), which the CPU tests pin to these rows.
+    # from the model on every ray
     import xenodon_gb300 as xg
     vols = {}
-    left_out = {c["volume"] for c in glsl_golden.cases if not glsl_golden.reproducible(c)}
-    assert left_out <= {"ct512"}, left_out
     for case in glsl_golden.cases:
-        if case["volume"] in left_out:
-            continue
         v = glsl_golden.view(case)
         trav = case["traversal"]
         key = (case["volume"], "grid" if trav == "dda" else case["tree"])
@@ -254,19 +246,13 @@ def test_cuda_matches_the_reference_shaders(ctx, glsl_golden):
         vol.release()
 
 
-def _golden_cases(glsl_golden):
-    left_out = {c["volume"] for c in glsl_golden.cases if not glsl_golden.reproducible(c)}
-    assert left_out <= {"ct512"}, left_out
-    return [c for c in glsl_golden.cases if c["volume"] not in left_out]
-
-
 def test_batch_matches_the_reference_shaders(ctx, glsl_golden):
     # the golden cases (as above) as one batch: the persistent batch kernel,
     # one launch over every case's warp tiles, gives the reference shaders'
     # RGBA8 pixels
     import torch
     import xenodon_gb300 as xg
-    cases = _golden_cases(glsl_golden)
+    cases = glsl_golden.cases
     vols, specs, bufs = {}, [], []
     for case in cases:
         v = glsl_golden.view(case)
@@ -298,7 +284,7 @@ def test_server_matches_the_reference_shaders(ctx, glsl_golden):
     # small frames fold into its running persistent kernel; every result is
     # the reference shaders' RGBA8 image
     import xenodon_gb300 as xg
-    cases = _golden_cases(glsl_golden)
+    cases = glsl_golden.cases
     ids = {}
     with xg.Server(ctx, max_batch_jobs=64, streams=2) as server:
         tickets = []

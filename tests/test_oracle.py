@@ -209,15 +209,9 @@ def test_oracle_matches_the_reference_shaders(oracle_lib, glsl_golden):
     # configuration at 512x512, and two rows of a frame from each leg of the
     # 512x361x512 CT configuration's path at 1920x1080.  The oracle's FP32
     # restatement must give the same RGBA8 pixels, the same float colour and
-    # the same count of words read from the model on every ray.  (A host
-    # whose CT generator rounds differently regenerates a slightly different
-    # full-size CT volume; its rows are left out there.)
+    # the same count of words read from the model on every ray.
     assert len(glsl_golden.cases) == 138
-    left_out = {c["volume"] for c in glsl_golden.cases if not glsl_golden.reproducible(c)}
-    assert left_out <= {"ct512"}, left_out
     for case in glsl_golden.cases:
-        if case["volume"] in left_out:
-            continue
         v = glsl_golden.view(case)
         dda = case["traversal"] == "dda"
         view = oracle_lib.make_view(v["width"], v["height"], v["emission"], v["ratio"], v["out_off"], v["out_ext"],

@@ -80,7 +80,10 @@ def ct_shell(dx: int = 512, dy: int = 361, dz: int = 512, seed: int = 1, device=
     A closed ellipsoidal shell with semi-axes 0.40/0.35/0.30 of the largest
     extent and a thickness of 3-6 voxels, its radius perturbed by 3-octave
     value noise of amplitude 0.05; the interior holds gray N(90, 20) clamped to
-    [1, 255] at 20% of its voxels; the background is 0."""
+    [1, 255] at 20% of its voxels; the background is 0.  The normal variate is
+    the sum of twelve hashed uniforms less 6 (Irwin-Hall), added one at a time
+    in float32, and the rest is integer hashing and single IEEE operations,
+    so the bytes are the same on every host and device."""
     dev = _device(device)
     ext = float(max(dx, dy, dz))
     a, b, c = 0.40 * ext, 0.35 * ext, 0.30 * ext
@@ -110,12 +113,13 @@ def ct_shell(dx: int = 512, dy: int = 361, dz: int = 512, seed: int = 1, device=
         zi = torch.arange(z0, z1, device=dev, dtype=torch.int64)[:, None, None]
         lin = (xi + dx * (yi + dy * zi)) & _M32
         h1 = _hash32(lin ^ ((seed * 0x9E3779B1 + 5) & _M32))
-        h2 = _hash32(h1 ^ 0x68E31DA4)
-        h3 = _hash32(h2 ^ 0x1B56C4E9)
         u1 = h1.to(f32) / 4294967296.0
-        u2 = (h2.to(f32) + 1.0) / 4294967297.0
-        u3 = h3.to(f32) / 4294967296.0
-        gauss = torch.sqrt(-2.0 * torch.log(u2)) * torch.cos(2 * math.pi * u3)
+        h, gauss = h1, None
+        for k in range(12):
+            h = _hash32(h ^ ((0x68E31DA4 + 0x1B56C4E9 * k) & _M32))
+            u = h.to(f32) / 4294967296.0
+            gauss = u if gauss is None else gauss + u
+        gauss = gauss - 6.0
         gray = (90.0 + 20.0 * gauss).round().clamp(1, 255)
         shell_val = (200.0 + 40.0 * _noise_fixed(xs, ys, zs, 4.0, seed, 8)).round().clamp(1, 255)
         v = torch.where(inner & (u1 < 0.2), gray, torch.zeros((), device=dev, dtype=f32))
