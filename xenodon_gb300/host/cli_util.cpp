@@ -387,6 +387,8 @@ std::string format_frame_name(const std::string& pat, uint64_t frame) {
     return out;
 }
 
+// "{}" of a double in fmt 5.3.0, the version the reference builds with
+// (subprojects/fmt.wrap): without FMT_USE_GRISU that is printf's %g
 std::string fmt_double(double v) {
     char buf[64];
     std::snprintf(buf, sizeof buf, "%g", v);
